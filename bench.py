@@ -1,0 +1,346 @@
+#!/usr/bin/env python
+"""Benchmark of the SPH grid step on one GB300: particle-steps/s.
+
+    python bench.py [--steps K] [--warmup W] [--gpus 1] [--form plain|f64] [--impl ours|reference]
+
+Workload: the 1,000,000-particle dam break (100^3 lattice at 0.5 h spacing, +-1% seeded
+jitter, anchored at the min corner of a 5 x 5 x 2.5 m box -- the 20^3 / 1 x 1 x 0.5 m
+scene scaled x5 to keep its fill), gravity -9.81, the reference's constants. A step is
+one pass of the whole step (grid build, density, forces + walls + integration) over all
+particles, launched through the C ABI.
+
+value : particle-steps/s with the state resident in HBM; L2 is flushed (a 512 MiB write)
+        before every timed step, and the step is timed with CUDA events on the
+        library's own stream.
+e2e   : the same metric through the public C ABI with pinned host buffers: every step
+        uploads positions and velocities, steps once, and downloads them.
+roofline: algorithmic bytes of the dominant kernel / its event-timed duration, against
+        the measured HBM copy bandwidth.
+cpu_baseline: the oracle (restatement of the reference's serial CPU step) on 1 host core
+        for a bounded sample of the same workload.
+--impl reference: the same restatement on all host cores (OpenMP over particles, the
+        grid re-binning serial as in the reference), the same workload and metric.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "gmu-water-simulation_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s, mixed vs plain FP32 on GB300 at stated FP64 error; % HBM peak"
+UNIT = "particle-steps/s"
+BOX = (5.0, 5.0, 2.5)
+DIMS = (100, 100, 100)
+GRAVITY = (0.0, -9.81, 0.0)
+SEED = 1
+H32 = np.float32(0.0457)
+KERNELS_PER_STEP = 7  # scan reduce/top/apply, slot, rank+permute, density, forces
+
+
+def workload_desc(form):
+    return {
+        "workload": "dam break, 1,000,000 particles (100^3 lattice, 0.5h spacing, +-1% jitter), "
+                    "box 5 x 5 x 2.5 m, 110 x 110 x 55 cells",
+        "form": form,
+        "particles": 1_000_000,
+        "cells": 665_500,
+        "steps_from": "initial lattice",
+        "l2": "flushed before every timed step (512 MiB write)",
+        "parallelism": "single GPU",
+    }
+
+
+def grid_cells(box):
+    return int(np.prod([int(np.ceil(np.float32(b) / H32)) for b in box]))
+
+
+def alg_bytes(N, C, rs=4):
+    """Compulsory DRAM bytes of each kernel of one step: every array it must touch,
+    read or written once (neighbour re-reads are cache hits). rs = bytes per real."""
+    r4 = 4 * rs
+    return {
+        # counts read twice, starts/cursors written, counts zeroed
+        "scan": 20 * C,
+        # (cell, id) read, id scattered, cursor read-modify-write
+        "slot": 12 * N + 8 * C,
+        # (cell, id) + the cell's ids read, state read and written in sorted order, starts
+        "rank_permute": 8 * N + 4 * N + 4 * r4 * N + 4 * C,
+        # sorted positions read, (rho, p, p/rho^2, 1/rho) written, row starts
+        "density": r4 * N + r4 * N + 4 * C,
+        # own position, velocity, aux read; new position, velocity, (cell, id) written;
+        # row starts read; counts read-modify-write
+        "forces": 3 * r4 * N + 2 * r4 * N + 8 * N + 12 * C,
+    }
+
+
+def load_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region (read-only queries)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks.csv") if os.path.isdir(
+            os.path.join(ROOT, "gpurun_out")) else "/tmp/sph_bench_clocks.csv"
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(pos, steps_budget_s=12.0, threads=1):
+    """The oracle on `threads` host cores: steps of the same scene until the budget is used."""
+    from oracle import oracle as O
+
+    o = O.Oracle(BOX, O.REF, threads=threads, gravity=GRAVITY)
+    o.add(pos)
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        o.step(1)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= steps_budget_s or n >= 20:
+            break
+    o.close()
+    return pos.shape[0] * n / el, n, el
+
+
+def run_reference(args):
+    """--impl reference: the oracle restatement of the reference's CPU step on all cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import sphcuda
+    from oracle import oracle as O
+
+    O.build()
+    pos = sphcuda.dam_break_scene(DIMS, BOX, SEED)
+    threads = os.cpu_count() or 1
+    o = O.Oracle(BOX, O.REF, threads=threads, gravity=GRAVITY)
+    o.add(pos)
+    for _ in range(args.warmup):
+        o.step(1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step(1)
+    el = time.perf_counter() - t0
+    value = pos.shape[0] * args.steps / el
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * el / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_desc("reference CPU step (oracle restatement), float/double as the reference"),
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} steps of the 1,000,000-particle dam break after {args.warmup} "
+                                   f"warm-up steps; density/force passes on {threads} threads (bit-identical to "
+                                   "1 thread), grid re-binning serial"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="plain", choices=["plain", "f64"])
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
+        print(json.dumps({"error": "this benchmark runs on one GPU (single-scene path; no multi-GPU path)"}))
+        return 2
+    args.warmup = max(args.warmup, 3)
+
+    import torch
+
+    import sphcuda
+
+    sphcuda.load()
+    form = {"plain": sphcuda.SPH_PLAIN_F32, "f64": sphcuda.SPH_F64}[args.form]
+    rs = 8 if args.form == "f64" else 4
+    pos = sphcuda.dam_break_scene(DIMS, BOX, SEED)
+    N = pos.shape[0]
+    C = grid_cells(BOX)
+    dev = torch.device("cuda:0")
+    torch.cuda.init()
+
+    ctx = sphcuda.SphContext(BOX, N, precision=form, gravity=GRAVITY)
+    ctx.upload(pos)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def one_step(evs=None):
+        if evs is not None:
+            evs[0].record(ext)
+        ctx.pass_grid()
+        if evs is not None:
+            evs[1].record(ext)
+        ctx.pass_density()
+        if evs is not None:
+            evs[2].record(ext)
+        ctx.pass_forces()
+        if evs is not None:
+            evs[3].record(ext)
+
+    for _ in range(args.warmup):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        one_step()
+    torch.cuda.synchronize()
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        one_step(evs[k])
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    grid_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    dens_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    forc_ms = [e[2].elapsed_time(e[3]) for e in evs]
+    step_ms = [e[0].elapsed_time(e[3]) for e in evs]
+    total_ms = sum(step_ms)
+    value = N * args.steps / (total_ms / 1000.0)
+    stats = ctx.stats()
+    assert stats["count"] == N and np.isfinite(stats["rho_mean"])
+
+    ab = alg_bytes(N, C, rs)
+    peak, peak_src = load_peak()
+    mean = lambda xs: sum(xs) / len(xs)
+    dom = "forces" if mean(forc_ms) >= mean(dens_ms) else "density"
+    dom_ms = mean(forc_ms) if dom == "forces" else mean(dens_ms)
+    achieved = ab[dom] / (dom_ms / 1000.0) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(f"k_{dom}", {}).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+    step_bytes = sum(ab.values())
+
+    # ---- end to end through the C ABI with pinned host buffers
+    # two pinned (xyz, vel) pairs: each step uploads one and downloads into the other
+    bufs = [(torch.from_numpy(pos.copy()).pin_memory(), torch.zeros((N, 3), dtype=torch.float32).pin_memory()),
+            (torch.empty((N, 3), dtype=torch.float32).pin_memory(),
+             torch.empty((N, 3), dtype=torch.float32).pin_memory())]
+    counts = np.array([N], np.uint32)
+
+    def e2e_step(k):
+        src, dst = bufs[k % 2], bufs[(k + 1) % 2]
+        ctx.upload_raw(src[0].data_ptr(), src[1].data_ptr(), counts)
+        ctx.step(1)
+        ctx.download_raw(dst[0].data_ptr(), dst[1].data_ptr())
+
+    for k in range(2):
+        e2e_step(k)
+    t0 = time.perf_counter()
+    for k in range(args.e2e_steps):
+        e2e_step(k)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": N * args.e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 24 * N,
+           "d2h_bytes_per_step": 24 * N,
+           "path": "sph_upload (pinned xyz+vel) -> sph_step(1) -> sph_download (pinned xyz+vel), host timer"}
+    ctx.close()
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, n, el = cpu_baseline(pos, args.cpu_budget, threads=1)
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"first {n} steps of the same 1,000,000-particle dam break, oracle restatement of the "
+                         f"reference's serial CPU step, 1 thread, {el:.1f} s"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.form == "f64" else "f32", "data": "synthetic (seeded lattice, no dataset)",
+        "config": workload_desc({"plain": "plain FP32", "f64": "FP64"}[args.form]),
+        "roofline": {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+                     "alg_bytes_per_launch": ab[dom], "launch_ms": dom_ms},
+        "step_roofline": {"alg_bytes_per_step": step_bytes, "achieved_gbs": step_bytes / (total_ms / args.steps / 1000) / 1e9,
+                          "frac": step_bytes / (total_ms / args.steps / 1000) / 1e9 / peak},
+        "passes_ms": {"grid": mean(grid_ms), "density": mean(dens_ms), "forces": mean(forc_ms)},
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "gpu_launches": KERNELS_PER_STEP * args.steps,
+        "clocks": clk,
+        "wall_s_timed_region": t_wall,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

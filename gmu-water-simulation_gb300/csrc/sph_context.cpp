@@ -1,0 +1,754 @@
+// sph_context.cpp -- host side of the C ABI (include/sph_cuda.h): context, buffers,
+// pass sequencing, CUDA-graph replay of whole steps, transfers and error reporting.
+//
+// Replaces CGPUBaseParticleSimulator / CGPUParticleSimulator and CLWrapper
+// (src/CGPUBaseParticleSimulator.cpp, src/CGPUParticleSimulator.cpp, src/CLWrapper.cpp):
+// one CUDA stream per context instead of one OpenCL queue, the whole step on the device
+// instead of a host sort and four full-array copies per step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/sph_cuda.h"
+#include "sph_internal.h"
+
+using namespace sph;
+
+namespace {
+
+struct SceneHost {
+    float box[3];
+    int32_t res[3];
+    uint32_t cell_base, ncells, cap, count;
+    float gravity[3];
+    std::vector<ObstacleDev> obs;
+};
+
+enum State { EMPTY = 0, HASHED = 1, SORTED = 2, DENSE = 3 };
+
+thread_local std::string g_create_error;
+
+}  // namespace
+
+struct sph_ctx {
+    sph_params prm{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<SceneHost> sc;
+    uint64_t ctot = 0, ncap = 0;
+    uint32_t n = 0;         // particles held (including appended ones)
+    uint32_t n_sorted = 0;  // particles covered by the last grid pass
+    uint32_t n_forced = 0;  // particles covered by the last force pass (recorded accelerations)
+    uint32_t n_dense = 0;   // particles covered by the last density pass (valid aux records)
+    DevBufs b{};
+    void *pool = nullptr;
+    State state = EMPTY;
+    bool appended = false;  // particles appended since the last grid pass
+    std::string err, devname;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double ms[5] = {0, 0, 0, 0, 0};
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+    uint32_t graph_n = 0;
+    std::vector<uint32_t> scene_off_host;
+};
+
+namespace {
+
+int fail(sph_ctx *c, int code, const std::string &msg)
+{
+    if (c) c->err = msg;
+    else g_create_error = msg;
+    return code;
+}
+
+int cuda_fail(sph_ctx *c, cudaError_t e, const char *what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return fail(c, SPH_ERR_CUDA, m);
+}
+
+#define CK(ctx, call)                                               \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call);  \
+    } while (0)
+
+bool is_f64(const sph_ctx *c) { return c->prm.precision == SPH_F64; }
+size_t r4_bytes(const sph_ctx *c) { return is_f64(c) ? 32 : 16; }
+
+template <class R>
+Consts<R> make_consts(const sph_params &p)
+{
+    Consts<R> c{};
+    const double h = (double) p.h;
+    c.h = (R) p.h;
+    if (sizeof(R) == 4) c.h2 = (R) (p.h * p.h);  // float product, as h*h in the reference
+    else c.h2 = (R) (h * h);
+    c.mass = (R) p.mass;
+    c.k = (R) p.gas_stiffness;
+    c.rho0 = (R) p.rest_density;
+    c.mu = (R) p.viscosity;
+    c.dt = (R) p.dt;
+    c.c_poly6 = (R) (315.0 / (64.0 * M_PI * std::pow(h, 9)));
+    c.c_spiky = (R) (-45.0 / (M_PI * std::pow(h, 6)));
+    c.c_visc = (R) (45.0 / (M_PI * std::pow(h, 6)));
+    c.wall_k = (R) (double) p.wall_k;
+    c.wall_damp = sizeof(R) == 4 ? (R) p.wall_damping : (R) (p.wall_damping == -0.9f ? -0.9 : (double) p.wall_damping);
+    c.wall_r = sizeof(R) == 4 ? (R) p.wall_radius : (R) (p.wall_radius == 0.01f ? 0.01 : (double) p.wall_radius);
+    c.h_f = p.h;
+    c.inv_h_f = 1.0f / p.h;
+    c.h_d = (double) p.h;
+    return c;
+}
+
+int upload_scenes(sph_ctx *c)
+{
+    std::vector<SceneDev> sd(c->sc.size());
+    uint32_t ob = 0;
+    for (size_t s = 0; s < c->sc.size(); s++) {
+        const SceneHost &h = c->sc[s];
+        SceneDev &d = sd[s];
+        std::memset(&d, 0, sizeof(d));
+        for (int a = 0; a < 3; a++) {
+            d.half[a] = h.box[a] / 2.0f;
+            d.res[a] = h.res[a];
+            d.gravity[a] = h.gravity[a];
+        }
+        d.cell_base = h.cell_base;
+        d.ncells = h.ncells;
+        d.obs_base = ob;
+        d.n_obs = (uint32_t) h.obs.size();
+        ob += d.n_obs;
+    }
+    CK(c, cudaMemcpyAsync(c->b.scenes, sd.data(), sd.size() * sizeof(SceneDev), cudaMemcpyHostToDevice, c->stream));
+    if (ob) {
+        std::vector<ObstacleDev> all;
+        for (auto &h : c->sc) all.insert(all.end(), h.obs.begin(), h.obs.end());
+        CK(c, cudaMemcpyAsync(c->b.obstacles, all.data(), all.size() * sizeof(ObstacleDev), cudaMemcpyHostToDevice,
+                              c->stream));
+    }
+    CK(c, cudaStreamSynchronize(c->stream));
+    return SPH_OK;
+}
+
+int upload_scene_off(sph_ctx *c)
+{
+    c->scene_off_host.assign(c->sc.size() + 1, 0);
+    for (size_t s = 0; s < c->sc.size(); s++) c->scene_off_host[s + 1] = c->scene_off_host[s] + c->sc[s].count;
+    CK(c, cudaMemcpyAsync(c->b.scene_off, c->scene_off_host.data(), c->scene_off_host.size() * sizeof(uint32_t),
+                          cudaMemcpyHostToDevice, c->stream));
+    return SPH_OK;
+}
+
+void drop_graph(sph_ctx *c)
+{
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    c->graph_steps = 0;
+}
+
+int allocate(sph_ctx *c)
+{
+    const size_t r4 = r4_bytes(c), rs = is_f64(c) ? 8 : 4;
+    const uint64_t N = c->ncap, C = c->ctot;
+    const uint64_t nb = (C + 4095) / 4096 + 1;
+    uint64_t nobs = 0;
+    for (auto &h : c->sc) nobs += h.obs.size();
+    struct Item { void **p; size_t bytes; };
+    DevBufs &b = c->b;
+    const bool rec = (c->prm.flags & SPH_FLAG_RECORD_ACC) != 0;
+    std::vector<Item> items = {
+        {&b.pos_s, r4 * N}, {&b.vel_s, r4 * N}, {&b.pos_u, r4 * N}, {&b.vel_u, r4 * N}, {&b.aux, r4 * N},
+        {&b.acc, rec ? r4 * N : 0},
+        {(void **) &b.cid_u, 8 * N}, {(void **) &b.tmp, 4 * N},
+        {(void **) &b.count, 4 * C}, {(void **) &b.start, 4 * (C + 1)}, {(void **) &b.cursor, 4 * C},
+        {(void **) &b.bsum, 4 * nb},
+        {(void **) &b.scenes, sizeof(SceneDev) * c->sc.size()},
+        {(void **) &b.obstacles, sizeof(ObstacleDev) * (nobs ? nobs : 1)},
+        {(void **) &b.scene_off, 4 * (c->sc.size() + 1)}, {(void **) &b.err, 16},
+        {(void **) &b.st_xyz, 12 * N}, {(void **) &b.st_vel, 12 * N},
+        {(void **) &b.st_rho, rs == 4 ? 4 * N : 0}, {(void **) &b.st_p, rs == 4 ? 4 * N : 0},
+        {(void **) &b.st_acc, rs == 4 && rec ? 12 * N : 0},
+        {(void **) &b.st_xyz64, rs == 8 ? 24 * N : 0}, {(void **) &b.st_vel64, rs == 8 ? 24 * N : 0},
+        {(void **) &b.st_rho64, rs == 8 ? 8 * N : 0}, {(void **) &b.st_p64, rs == 8 ? 8 * N : 0},
+        {(void **) &b.st_acc64, rs == 8 && rec ? 24 * N : 0},
+        {(void **) &b.stats, 64 * c->sc.size()},
+    };
+    size_t total = 0;
+    for (auto &it : items) total += (it.bytes + 255) & ~size_t(255);
+    cudaError_t e = cudaMalloc(&c->pool, total);
+    if (e != cudaSuccess) {
+        c->pool = nullptr;
+        return fail(c, SPH_ERR_NOMEM, std::string("device allocation of ") + std::to_string(total) +
+                                          " bytes failed: " + cudaGetErrorString(e));
+    }
+    char *p = (char *) c->pool;
+    for (auto &it : items) {
+        *it.p = it.bytes ? (void *) p : nullptr;
+        p += (it.bytes + 255) & ~size_t(255);
+    }
+    CK(c, cudaMemsetAsync(b.count, 0, 4 * C, c->stream));
+    CK(c, cudaMemsetAsync(b.aux, 0, r4 * N, c->stream));
+    CK(c, cudaMemsetAsync(b.err, 0, 16, c->stream));
+    return SPH_OK;
+}
+
+int create_common(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *scenes, sph_ctx **out)
+{
+    if (!out) return fail(nullptr, SPH_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (!p || !scenes || n_scenes == 0) return fail(nullptr, SPH_ERR_ARG, "params/scenes missing or n_scenes == 0");
+    if (p->struct_size != sizeof(sph_params)) return fail(nullptr, SPH_ERR_ARG, "sph_params.struct_size mismatch");
+    if (!(p->h > 0) || !(p->dt > 0) || !(p->mass > 0)) return fail(nullptr, SPH_ERR_ARG, "h, dt and mass must be > 0");
+    if (p->precision != SPH_PLAIN_F32 && p->precision != SPH_F64)
+        return fail(nullptr, SPH_ERR_UNSUPPORTED, "precision form not available in this build");
+    sph_ctx *c = new (std::nothrow) sph_ctx();
+    if (!c) return fail(nullptr, SPH_ERR_NOMEM, "host allocation failed");
+    c->prm = *p;
+    c->device = p->device;
+    uint64_t ctot = 0, ncap = 0;
+    for (uint32_t s = 0; s < n_scenes; s++) {
+        const sph_scene_desc &d = scenes[s];
+        SceneHost h{};
+        for (int a = 0; a < 3; a++) {
+            if (!(d.box[a] > 0) || !std::isfinite(d.box[a])) {
+                delete c;
+                return fail(nullptr, SPH_ERR_ARG, "scene " + std::to_string(s) + ": box extents must be finite and > 0");
+            }
+            h.box[a] = d.box[a];
+            h.res[a] = (int32_t) std::ceil(d.box[a] / p->h);  // float division, then ceil
+            h.gravity[a] = p->gravity[a];
+        }
+        const uint64_t nc = (uint64_t) h.res[0] * h.res[1] * h.res[2];
+        h.cell_base = (uint32_t) ctot;
+        h.ncells = (uint32_t) nc;
+        h.cap = d.max_particles;
+        h.count = 0;
+        if (d.n_obstacles && !d.obstacles) {
+            delete c;
+            return fail(nullptr, SPH_ERR_ARG, "scene " + std::to_string(s) + ": obstacles pointer is NULL");
+        }
+        for (uint32_t o = 0; o < d.n_obstacles; o++) {
+            ObstacleDev ob{};
+            for (int a = 0; a < 3; a++) {
+                ob.lo[a] = d.obstacles[6 * o + a];
+                ob.hi[a] = d.obstacles[6 * o + 3 + a];
+            }
+            h.obs.push_back(ob);
+        }
+        ctot += nc;
+        ncap += d.max_particles;
+        c->sc.push_back(h);
+    }
+    if (ctot >= (1ull << 31) || ncap >= (1ull << 31) || ncap == 0) {
+        delete c;
+        return fail(nullptr, SPH_ERR_ARG, "total cells and particle capacity must be in [1, 2^31)");
+    }
+    c->ctot = ctot;
+    c->ncap = ncap;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        std::string m = std::string("CUDA device ") + std::to_string(c->device) + " unavailable: " + cudaGetErrorString(e);
+        delete c;
+        return fail(nullptr, SPH_ERR_CUDA, m);
+    }
+    for (auto &ev : c->ev) cudaEventCreate(&ev);
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, c->device) == cudaSuccess) {
+        char buf[512];
+        std::snprintf(buf, sizeof buf, "%s (CUDA sm_%d%d, %d SMs)", prop.name, prop.major, prop.minor,
+                      prop.multiProcessorCount);
+        c->devname = buf;
+    }
+    int rc = allocate(c);
+    if (rc == SPH_OK) rc = upload_scenes(c);
+    if (rc == SPH_OK) rc = upload_scene_off(c);
+    if (rc == SPH_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = fail(c, SPH_ERR_CUDA, "setup failed");
+    if (rc != SPH_OK) {
+        g_create_error = c->err;
+        sph_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return SPH_OK;
+}
+
+template <class R>
+int run_grid(sph_ctx *c)
+{
+    CK(c, Launch<R>::scan(c->b, (uint32_t) c->ctot, c->stream));
+    CK(c, Launch<R>::permute(c->b, c->n, c->stream));
+    return SPH_OK;
+}
+template <class R>
+int run_density(sph_ctx *c)
+{
+    CK(c, Launch<R>::density(c->b, c->n, make_consts<R>(c->prm), c->stream));
+    return SPH_OK;
+}
+template <class R>
+int run_forces(sph_ctx *c)
+{
+    CK(c, Launch<R>::forces(c->b, c->n, make_consts<R>(c->prm), (c->prm.flags & SPH_FLAG_RECORD_ACC) != 0,
+                            c->stream));
+    return SPH_OK;
+}
+
+int pass_grid(sph_ctx *c)
+{
+    if (c->state != HASHED) return fail(c, SPH_ERR_STATE, "grid pass needs hashed particles (upload first)");
+    int rc = is_f64(c) ? run_grid<double>(c) : run_grid<float>(c);
+    if (rc) return rc;
+    c->state = SORTED;
+    c->n_sorted = c->n;
+    c->appended = false;
+    return SPH_OK;
+}
+int pass_density(sph_ctx *c)
+{
+    if (c->state != SORTED) return fail(c, SPH_ERR_STATE, "density pass must follow the grid pass");
+    int rc = is_f64(c) ? run_density<double>(c) : run_density<float>(c);
+    if (rc) return rc;
+    c->state = DENSE;
+    c->n_dense = c->n;
+    return SPH_OK;
+}
+int pass_forces(sph_ctx *c)
+{
+    if (c->state != DENSE) return fail(c, SPH_ERR_STATE, "force pass must follow the density pass");
+    int rc = is_f64(c) ? run_forces<double>(c) : run_forces<float>(c);
+    if (rc) return rc;
+    c->state = HASHED;
+    c->n_forced = c->n;
+    return SPH_OK;
+}
+
+int one_step(sph_ctx *c)
+{
+    int rc = pass_grid(c);
+    if (!rc) rc = pass_density(c);
+    if (!rc) rc = pass_forces(c);
+    return rc;
+}
+
+// Steps per captured graph: small scenes are launch-bound, so one graph holds several steps.
+int graph_unroll(uint32_t n) { return n < 262144 ? 8 : 2; }
+
+int build_graph(sph_ctx *c, int steps)
+{
+    drop_graph(c);
+    CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = SPH_OK;
+    for (int k = 0; k < steps && rc == SPH_OK; k++) rc = one_step(c);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        c->graph = nullptr;
+        return cuda_fail(c, e, "cudaGraphInstantiate");
+    }
+    c->graph_steps = steps;
+    c->graph_n = c->n;
+    return SPH_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) ms = 0;
+    return ms;
+}
+
+}  // namespace
+
+// =====================================================================================
+extern "C" {
+
+void sph_params_default(sph_params *p)
+{
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->struct_size = sizeof(sph_params);
+    p->h = 0.0457f;            // include/CParticle.h:80
+    p->viscosity = 3.5f;       // :81
+    p->mass = 0.02f;           // :82
+    p->gas_stiffness = 3.0f;   // :83
+    p->rest_density = 998.29f; // :84
+    p->dt = 0.01f;             // src/CBaseParticleSimulator.cpp:7
+    p->gravity[0] = 0.0f;
+    p->gravity[1] = -9.80665f; // include/CBaseParticleSimulator.h:19
+    p->gravity[2] = 0.0f;
+    p->wall_k = 10000.0f;      // include/CCollisionGeometry.h:20
+    p->wall_damping = -0.9f;   // include/CCollisionGeometry.h:21
+    p->wall_radius = 0.01f;    // src/CCollisionGeometry.cpp:124
+    p->precision = SPH_PLAIN_F32;
+    p->flags = 0;
+    p->device = 0;
+}
+
+int sph_create(const sph_params *p, const float box[3], uint32_t max_particles, sph_ctx **out)
+{
+    try {
+        if (!box) return fail(nullptr, SPH_ERR_ARG, "box is NULL");
+        sph_scene_desc d{};
+        for (int a = 0; a < 3; a++) d.box[a] = box[a];
+        d.max_particles = max_particles;
+        return create_common(p, 1, &d, out);
+    } catch (...) {
+        return fail(nullptr, SPH_ERR_NOMEM, "host exception in sph_create");
+    }
+}
+
+int sph_batch_create(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *scenes, sph_ctx **out)
+{
+    try {
+        return create_common(p, n_scenes, scenes, out);
+    } catch (...) {
+        return fail(nullptr, SPH_ERR_NOMEM, "host exception in sph_batch_create");
+    }
+}
+
+void sph_destroy(sph_ctx *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    drop_graph(c);
+    for (auto &ev : c->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (c->pool) cudaFree(c->pool);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char *sph_last_error(const sph_ctx *c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+const char *sph_device_name(const sph_ctx *c) { return c ? c->devname.c_str() : ""; }
+
+void *sph_stream(const sph_ctx *c) { return c ? (void *) c->stream : nullptr; }
+
+int sph_upload(sph_ctx *c, const float *xyz, const float *vel, const uint32_t *counts)
+{
+    if (!c) return SPH_ERR_ARG;
+    try {
+        if (!counts) return fail(c, SPH_ERR_ARG, "counts is NULL");
+        uint64_t total = 0;
+        for (size_t s = 0; s < c->sc.size(); s++) {
+            if (counts[s] > c->sc[s].cap)
+                return fail(c, SPH_ERR_CAPACITY, "scene " + std::to_string(s) + ": " + std::to_string(counts[s]) +
+                                                     " particles exceed its capacity " + std::to_string(c->sc[s].cap));
+            total += counts[s];
+        }
+        if (total && !xyz) return fail(c, SPH_ERR_ARG, "xyz is NULL");
+        CK(c, cudaSetDevice(c->device));
+        drop_graph(c);
+        for (size_t s = 0; s < c->sc.size(); s++) c->sc[s].count = counts[s];
+        c->n = (uint32_t) total;
+        int rc = upload_scene_off(c);
+        if (rc) return rc;
+        CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
+        if (total) {
+            CK(c, cudaMemcpyAsync(c->b.st_xyz, xyz, 12 * total, cudaMemcpyHostToDevice, c->stream));
+            if (vel) CK(c, cudaMemcpyAsync(c->b.st_vel, vel, 12 * total, cudaMemcpyHostToDevice, c->stream));
+            if (is_f64(c))
+                CK(c, Launch<double>::ingest(c->b, c->b.st_xyz, vel ? c->b.st_vel : nullptr, 0, c->n, -1, 0,
+                                             (uint32_t) c->sc.size(), make_consts<double>(c->prm), c->stream));
+            else
+                CK(c, Launch<float>::ingest(c->b, c->b.st_xyz, vel ? c->b.st_vel : nullptr, 0, c->n, -1, 0,
+                                            (uint32_t) c->sc.size(), make_consts<float>(c->prm), c->stream));
+        }
+        c->state = HASHED;
+        c->n_sorted = 0;
+        c->n_forced = 0;
+        c->n_dense = 0;
+        c->appended = false;
+        return SPH_OK;
+    } catch (...) {
+        return fail(c, SPH_ERR_NOMEM, "host exception in sph_upload");
+    }
+}
+
+int sph_append(sph_ctx *c, uint32_t scene, const float *xyz, const float *vel, uint32_t n)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (scene >= c->sc.size()) return fail(c, SPH_ERR_ARG, "scene index out of range");
+    if (n == 0) return SPH_OK;
+    if (!xyz) return fail(c, SPH_ERR_ARG, "xyz is NULL");
+    if (c->state != HASHED) return fail(c, SPH_ERR_STATE, "append needs a completed step (or an upload) first");
+    SceneHost &h = c->sc[scene];
+    if ((uint64_t) h.count + n > h.cap)
+        return fail(c, SPH_ERR_CAPACITY, "scene " + std::to_string(scene) + " would exceed its capacity");
+    CK(c, cudaSetDevice(c->device));
+    drop_graph(c);
+    CK(c, cudaMemcpyAsync(c->b.st_xyz, xyz, 12ull * n, cudaMemcpyHostToDevice, c->stream));
+    if (vel) CK(c, cudaMemcpyAsync(c->b.st_vel, vel, 12ull * n, cudaMemcpyHostToDevice, c->stream));
+    if (is_f64(c))
+        CK(c, Launch<double>::ingest(c->b, c->b.st_xyz, vel ? c->b.st_vel : nullptr, c->n, n, (int32_t) scene, h.count,
+                                     (uint32_t) c->sc.size(), make_consts<double>(c->prm), c->stream));
+    else
+        CK(c, Launch<float>::ingest(c->b, c->b.st_xyz, vel ? c->b.st_vel : nullptr, c->n, n, (int32_t) scene, h.count,
+                                    (uint32_t) c->sc.size(), make_consts<float>(c->prm), c->stream));
+    // the staging buffers are reused by the next transfer: finish this one first
+    CK(c, cudaStreamSynchronize(c->stream));
+    h.count += n;
+    c->n += n;
+    c->appended = true;
+    return SPH_OK;
+}
+
+int sph_set_gravity(sph_ctx *c, int32_t scene, const float g[3])
+{
+    if (!c || !g) return c ? fail(c, SPH_ERR_ARG, "gravity is NULL") : SPH_ERR_ARG;
+    if (scene >= (int32_t) c->sc.size()) return fail(c, SPH_ERR_ARG, "scene index out of range");
+    for (size_t s = 0; s < c->sc.size(); s++)
+        if (scene < 0 || (size_t) scene == s)
+            for (int a = 0; a < 3; a++) c->sc[s].gravity[a] = g[a];
+    CK(c, cudaSetDevice(c->device));
+    return upload_scenes(c);
+}
+
+// Pass-by-pass calls; with SPH_FLAG_PROFILE each records CUDA events around its work and
+// the force pass resolves the three times (sProfilingEvent's grid, density, forces fields).
+int sph_pass_grid(sph_ctx *c)
+{
+    if (!c) return SPH_ERR_ARG;
+    CK(c, cudaSetDevice(c->device));
+    const bool prof = (c->prm.flags & SPH_FLAG_PROFILE) != 0;
+    if (prof) CK(c, cudaEventRecord(c->ev[0], c->stream));
+    int rc = pass_grid(c);
+    if (!rc && prof) CK(c, cudaEventRecord(c->ev[1], c->stream));
+    return rc;
+}
+int sph_pass_density(sph_ctx *c)
+{
+    if (!c) return SPH_ERR_ARG;
+    CK(c, cudaSetDevice(c->device));
+    int rc = pass_density(c);
+    if (!rc && (c->prm.flags & SPH_FLAG_PROFILE)) CK(c, cudaEventRecord(c->ev[2], c->stream));
+    return rc;
+}
+int sph_pass_forces(sph_ctx *c)
+{
+    if (!c) return SPH_ERR_ARG;
+    CK(c, cudaSetDevice(c->device));
+    int rc = pass_forces(c);
+    if (!rc && (c->prm.flags & SPH_FLAG_PROFILE)) {
+        CK(c, cudaEventRecord(c->ev[3], c->stream));
+        CK(c, cudaEventSynchronize(c->ev[3]));
+        c->ms[0] = elapsed(c->ev[0], c->ev[1]);
+        c->ms[1] = elapsed(c->ev[1], c->ev[2]);
+        c->ms[2] = elapsed(c->ev[2], c->ev[3]);
+        c->ms[3] = 0;
+        c->ms[4] = 0;
+    }
+    return rc;
+}
+
+int sph_step(sph_ctx *c, int32_t nsteps)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (nsteps < 0) return fail(c, SPH_ERR_ARG, "nsteps < 0");
+    if (c->state != HASHED) return fail(c, SPH_ERR_STATE, "step needs uploaded particles and no pass in progress");
+    CK(c, cudaSetDevice(c->device));
+    if (c->prm.flags & SPH_FLAG_PROFILE) {
+        for (int k = 0; k < nsteps; k++) {
+            CK(c, cudaEventRecord(c->ev[0], c->stream));
+            int rc = pass_grid(c);
+            if (rc) return rc;
+            CK(c, cudaEventRecord(c->ev[1], c->stream));
+            rc = pass_density(c);
+            if (rc) return rc;
+            CK(c, cudaEventRecord(c->ev[2], c->stream));
+            rc = pass_forces(c);
+            if (rc) return rc;
+            CK(c, cudaEventRecord(c->ev[3], c->stream));
+        }
+        if (nsteps > 0) {
+            CK(c, cudaEventSynchronize(c->ev[3]));
+            c->ms[0] = elapsed(c->ev[0], c->ev[1]);
+            c->ms[1] = elapsed(c->ev[1], c->ev[2]);
+            c->ms[2] = elapsed(c->ev[2], c->ev[3]);
+            c->ms[3] = 0;
+            c->ms[4] = 0;
+        }
+        return SPH_OK;
+    }
+    const int unroll = graph_unroll(c->n);
+    int done = 0;
+    if (nsteps >= unroll) {
+        if (!c->graph || c->graph_steps != unroll || c->graph_n != c->n) {
+            int rc = build_graph(c, unroll);
+            if (rc) return rc;
+            c->state = HASHED;
+        }
+        while (nsteps - done >= unroll) {
+            CK(c, cudaGraphLaunch(c->graph, c->stream));
+            done += unroll;
+        }
+        c->n_sorted = c->n_dense = c->n_forced = c->n;
+        c->appended = false;
+    }
+    for (; done < nsteps; done++) {
+        int rc = one_step(c);
+        if (rc) return rc;
+    }
+    CK(c, cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_pass_times(sph_ctx *c, double ms[5])
+{
+    if (!c || !ms) return SPH_ERR_ARG;
+    if (!(c->prm.flags & SPH_FLAG_PROFILE)) return fail(c, SPH_ERR_STATE, "context created without SPH_FLAG_PROFILE");
+    for (int k = 0; k < 5; k++) ms[k] = c->ms[k];
+    return SPH_OK;
+}
+
+int sph_get_counts(const sph_ctx *c, uint32_t *counts)
+{
+    if (!c || !counts) return SPH_ERR_ARG;
+    for (size_t s = 0; s < c->sc.size(); s++) counts[s] = c->sc[s].count;
+    return SPH_OK;
+}
+
+uint32_t sph_num_scenes(const sph_ctx *c) { return c ? (uint32_t) c->sc.size() : 0; }
+uint64_t sph_num_particles(const sph_ctx *c) { return c ? c->n : 0; }
+
+int sph_get_resolution(const sph_ctx *c, uint32_t scene, int32_t res[3])
+{
+    if (!c || !res || scene >= c->sc.size()) return SPH_ERR_ARG;
+    for (int a = 0; a < 3; a++) res[a] = c->sc[scene].res[a];
+    return SPH_OK;
+}
+
+static int download_impl(sph_ctx *c, void *xyz, void *vel, void *rho, void *p, void *acc, bool f64)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (f64 != is_f64(c)) return fail(c, SPH_ERR_ARG, f64 ? "context is not FP64" : "FP64 context: use sph_download_f64");
+    if (c->state == EMPTY) return fail(c, SPH_ERR_STATE, "nothing uploaded");
+    if (acc && !(c->prm.flags & SPH_FLAG_RECORD_ACC))
+        return fail(c, SPH_ERR_STATE, "accelerations need SPH_FLAG_RECORD_ACC");
+    CK(c, cudaSetDevice(c->device));
+    int rc = upload_scene_off(c);
+    if (rc) return rc;
+    const int layout_sorted = (c->state == SORTED || c->state == DENSE) ? 1 : 0;
+    const int aux_sorted = c->state == DENSE ? 1 : 0;
+    const size_t rs = f64 ? 8 : 4;
+    const uint32_t n = c->n;
+    DevBufs &b = c->b;
+    void *sx = f64 ? (void *) b.st_xyz64 : (void *) b.st_xyz;
+    void *sv = f64 ? (void *) b.st_vel64 : (void *) b.st_vel;
+    void *sr = f64 ? (void *) b.st_rho64 : (void *) b.st_rho;
+    void *sp = f64 ? (void *) b.st_p64 : (void *) b.st_p;
+    void *sa = f64 ? (void *) b.st_acc64 : (void *) b.st_acc;
+    CK(c, cudaMemsetAsync(sr, 0, rs * n, c->stream));
+    CK(c, cudaMemsetAsync(sp, 0, rs * n, c->stream));
+    if (sa) CK(c, cudaMemsetAsync(sa, 0, 3 * rs * n, c->stream));
+    // particles appended after the last grid pass have no density yet (0, as addParticle
+    // sets) and no acceleration
+    // aux records are indexed like the *_u arrays except right after a density pass
+    const uint32_t n_aux = c->n_dense;
+    const uint32_t n_acc = c->n_forced;
+    if (f64) CK(c, Launch<double>::egress(b, n, n_aux, n_acc, layout_sorted, aux_sorted, c->stream));
+    else CK(c, Launch<float>::egress(b, n, n_aux, n_acc, layout_sorted, aux_sorted, c->stream));
+    if (xyz) CK(c, cudaMemcpyAsync(xyz, sx, 3 * rs * n, cudaMemcpyDeviceToHost, c->stream));
+    if (vel) CK(c, cudaMemcpyAsync(vel, sv, 3 * rs * n, cudaMemcpyDeviceToHost, c->stream));
+    if (rho) CK(c, cudaMemcpyAsync(rho, sr, rs * n, cudaMemcpyDeviceToHost, c->stream));
+    if (p) CK(c, cudaMemcpyAsync(p, sp, rs * n, cudaMemcpyDeviceToHost, c->stream));
+    if (acc) CK(c, cudaMemcpyAsync(acc, sa, 3 * rs * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return SPH_OK;
+}
+
+int sph_download(sph_ctx *c, float *xyz, float *vel, float *rho, float *p, float *acc)
+{
+    try {
+        return download_impl(c, xyz, vel, rho, p, acc, false);
+    } catch (...) {
+        return fail(c, SPH_ERR_NOMEM, "host exception in sph_download");
+    }
+}
+
+int sph_download_f64(sph_ctx *c, double *xyz, double *vel, double *rho, double *p, double *acc)
+{
+    try {
+        return download_impl(c, xyz, vel, rho, p, acc, true);
+    } catch (...) {
+        return fail(c, SPH_ERR_NOMEM, "host exception in sph_download_f64");
+    }
+}
+
+int sph_get_grid(sph_ctx *c, uint32_t *cell_of_particle, uint32_t *cell_counts, uint32_t *sorted_ids)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (c->state != SORTED && c->state != DENSE) return fail(c, SPH_ERR_STATE, "the grid is available after a grid pass");
+    try {
+        CK(c, cudaSetDevice(c->device));
+        const uint32_t n = c->n;
+        std::vector<uint32_t> start(c->ctot + 1);
+        CK(c, cudaMemcpyAsync(start.data(), c->b.start, 4 * (c->ctot + 1), cudaMemcpyDeviceToHost, c->stream));
+        std::vector<uint2> cid(n);
+        if (n) CK(c, cudaMemcpyAsync(cid.data(), c->b.cid_u, 8ull * n, cudaMemcpyDeviceToHost, c->stream));
+        const size_t r4 = r4_bytes(c);
+        std::vector<unsigned char> vs((size_t) n * r4);
+        if (n) CK(c, cudaMemcpyAsync(vs.data(), c->b.vel_s, r4 * n, cudaMemcpyDeviceToHost, c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+        std::vector<uint32_t> off(c->sc.size() + 1, 0);
+        for (size_t s = 0; s < c->sc.size(); s++) off[s + 1] = off[s] + c->sc[s].count;
+        if (cell_counts)
+            for (uint64_t k = 0; k < c->ctot; k++) cell_counts[k] = start[k + 1] - start[k];
+        if (cell_of_particle) {
+            for (uint32_t i = 0; i < n; i++) {
+                const uint32_t cell = cid[i].x, id = cid[i].y;
+                size_t s = 0, hi = c->sc.size();
+                while (hi - s > 1) {  // last scene with cell_base <= cell
+                    size_t mid = (s + hi) / 2;
+                    if (c->sc[mid].cell_base <= cell) s = mid;
+                    else hi = mid;
+                }
+                cell_of_particle[off[s] + id] = cell - c->sc[s].cell_base;
+            }
+        }
+        if (sorted_ids) {
+            for (uint32_t k = 0; k < n; k++) {
+                uint32_t w;
+                std::memcpy(&w, vs.data() + (size_t) k * r4 + (r4 == 16 ? 12 : 24), 4);
+                sorted_ids[k] = w;
+            }
+        }
+        return SPH_OK;
+    } catch (...) {
+        return fail(c, SPH_ERR_NOMEM, "host exception in sph_get_grid");
+    }
+}
+
+int sph_stats(sph_ctx *c, uint32_t scene, double out[8])
+{
+    if (!c || !out) return SPH_ERR_ARG;
+    if (scene >= c->sc.size()) return fail(c, SPH_ERR_ARG, "scene index out of range");
+    if (!(c->state == HASHED && c->n_sorted > 0) && c->state != DENSE)
+        return fail(c, SPH_ERR_STATE, "statistics need a completed step or a density pass");
+    CK(c, cudaSetDevice(c->device));
+    const int layout_sorted = c->state == DENSE ? 1 : 0;
+    if (is_f64(c)) CK(c, Launch<double>::stats(c->b, (uint32_t) c->sc.size(), make_consts<double>(c->prm), layout_sorted, c->stream));
+    else CK(c, Launch<float>::stats(c->b, (uint32_t) c->sc.size(), make_consts<float>(c->prm), layout_sorted, c->stream));
+    CK(c, cudaMemcpyAsync(out, c->b.stats + 8 * scene, 64, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return SPH_OK;
+}
+
+}  // extern "C"

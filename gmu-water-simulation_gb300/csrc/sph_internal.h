@@ -1,0 +1,114 @@
+// sph_internal.h -- types shared by the host context and the sm_103a kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sph {
+
+// Device-side descriptor of one scene of a batch. Cells of scene s occupy the global
+// cell range [cell_base, cell_base + ncells); a scene's grid is (int) ceil(box / h) cells
+// per axis and its linear cell index is x + y*X + z*X*Y (include/CGrid.h:25-28).
+struct alignas(16) SceneDev {
+    float half[3];      // box / 2 (exact in float), the wall positions
+    uint32_t cell_base;
+    int32_t res[3];
+    uint32_t ncells;
+    float gravity[3];
+    uint32_t obs_base;  // first obstacle of this scene in the obstacle table
+    uint32_t n_obs;
+    uint32_t pad[3];
+};
+
+// Axis-aligned box obstacle: lo/hi corners.
+struct alignas(16) ObstacleDev {
+    float lo[3];
+    float pad0;
+    float hi[3];
+    float pad1;
+};
+
+// Step constants in the arithmetic type R (float for the plain form, double for FP64).
+template <class R>
+struct Consts {
+    R h, h2;           // smoothing length and its square
+    R mass, k, rho0, mu;
+    R dt;
+    R c_poly6, c_spiky, c_visc;  // 315/(64 pi h^9), -45/(pi h^6), 45/(pi h^6)
+    R wall_k, wall_damp, wall_r;
+    float h_f, inv_h_f; // float copies used by the cell hash (h as float, 1/h rounded)
+    double h_d;         // (double) h, divisor of the exact hash
+};
+
+// Buffers of one context, in the layout of the precision form.
+//   *_s : state in canonical sorted order, ascending (global cell, id)
+//   *_u : state in the previous sorted order (output of the force pass / upload)
+// .w of a position carries the scene index bits, .w of a velocity the particle id bits.
+struct DevBufs {
+    void *pos_s, *vel_s, *pos_u, *vel_u, *aux, *acc;  // R4 arrays
+    uint2 *cid_u;          // (global cell, id) of every *_u particle
+    uint32_t *tmp;         // ids scattered into cell slots, for the canonical rank
+    uint32_t *count;       // particles per global cell (hash output, zeroed by the scan)
+    uint32_t *start;       // exclusive scan of count, ncells_total + 1 entries
+    uint32_t *cursor;      // running slot per cell (starts at start[c])
+    uint32_t *bsum;        // scan block sums
+    SceneDev *scenes;
+    ObstacleDev *obstacles;
+    uint32_t *scene_off;   // first output index of every scene (id-order downloads)
+    int32_t *err;          // device error flag
+    // staging for host transfers (ingest / egress)
+    float *st_xyz, *st_vel, *st_rho, *st_p, *st_acc;
+    double *st_xyz64, *st_vel64, *st_rho64, *st_p64, *st_acc64;
+    double *stats;         // per-scene FP64 reductions, 8 doubles each
+};
+
+// ---- exact cell hash -------------------------------------------------------------
+// The reference computes floor((p + box/2.0) / h) in double (src/CCPUParticleSimulator.cpp:46-48)
+// and clamps to [0, res-1] (:50-69). Here the quotient is first taken in float; its
+// relative error is below 3 * 2^-24, so whenever it lies farther than 4e-7 * max(|q|, 1)
+// from an integer its floor equals the double result. Otherwise (and for NaN) the double
+// formula is evaluated exactly as the reference does. NaN and negatives map to cell 0,
+// values at or beyond res to res - 1.
+__host__ __device__ inline int cell_axis(float p, float half, float inv_h, double h_d, int res)
+{
+    const float qf = (p + half) * inv_h;
+    const float rq = rintf(qf);
+    if (fabsf(qf - rq) > fmaxf(fabsf(qf), 1.0f) * 4.0e-7f) {
+        if (qf < 0.0f) return 0;
+        if (qf >= (float) res) return res - 1;
+        return (int) floorf(qf);
+    }
+    const double q = ((double) p + (double) half) / h_d;
+    if (!(q >= 0.0)) return 0;
+    if (q >= (double) res) return res - 1;
+    return (int) floor(q);
+}
+
+__host__ __device__ inline int cell_axis(double p, float half, float inv_h, double h_d, int res)
+{
+    const double q = (p + (double) half) / h_d;
+    if (!(q >= 0.0)) return 0;
+    if (q >= (double) res) return res - 1;
+    return (int) floor(q);
+}
+
+// ---- kernel launchers (sph_kernels.cu) --------------------------------------------
+template <class R>
+struct Launch {
+    // xyz / vel: device staging arrays of n particles stored at [first, first + n).
+    // scene >= 0: all belong to that scene with ids id0..; scene < 0: scene and id follow
+    // the scene_off table (upload of every scene at once, first == 0).
+    static cudaError_t ingest(const DevBufs &b, const float *xyz, const float *vel, uint32_t first, uint32_t n,
+                              int32_t scene, uint32_t id0, uint32_t nscenes, Consts<R> c, cudaStream_t st);
+    static cudaError_t scan(const DevBufs &b, uint32_t ncells, cudaStream_t st);
+    static cudaError_t permute(const DevBufs &b, uint32_t n, cudaStream_t st);
+    static cudaError_t density(const DevBufs &b, uint32_t n, Consts<R> c, cudaStream_t st);
+    static cudaError_t forces(const DevBufs &b, uint32_t n, Consts<R> c, bool record_acc, cudaStream_t st);
+    // state of the first n_state particles, density/pressure of the first n_aux, and
+    // accelerations of the first n_acc (when recorded) into id-ordered staging arrays
+    static cudaError_t egress(const DevBufs &b, uint32_t n_state, uint32_t n_aux, uint32_t n_acc, int layout_sorted,
+                              int aux_sorted, cudaStream_t st);
+    static cudaError_t stats(const DevBufs &b, uint32_t nscenes, Consts<R> c, int layout_sorted, cudaStream_t st);
+};
+
+}  // namespace sph

@@ -1,0 +1,634 @@
+// sph_kernels.cu -- hand-written sm_103a kernels of the SPH grid step.
+//
+// One step is: scan (cell starts) -> slot + canonical rank + permute (sorted SoA)
+// -> density/pressure -> forces + walls + integration + next step's cell hash.
+// Semantics follow the reference's CPU simulator (src/CCPUParticleSimulator.cpp:32-229),
+// which the OpenCL grid path (resources/kernels/sph_grid.cl, sph_common.cl) approximates;
+// where the two differ (the OpenCL walls kernel's (1,1,0) start value, sph_common.cl:68,
+// and its float cell hash, sph_grid.cl:31-40) this follows the CPU path.
+//
+// All kernels are templated on the arithmetic type R: float is the plain form, double
+// the FP64 reference run of the same method.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sph_internal.h"
+
+namespace sph {
+
+template <class R>
+struct alignas(4 * sizeof(R)) Vec4 {
+    R x, y, z, w;
+};
+
+__device__ __forceinline__ Vec4<float> ld4(const Vec4<float> *p)
+{
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+    return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Vec4<double> ld4(const Vec4<double> *p)
+{
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+    const double2 a = __ldg(q), b = __ldg(q + 1);
+    return {a.x, a.y, b.x, b.y};
+}
+// plain (coherent) loads for buffers written earlier in the same kernel sequence
+__device__ __forceinline__ Vec4<float> ldc4(const Vec4<float> *p)
+{
+    const float4 v = *reinterpret_cast<const float4 *>(p);
+    return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Vec4<double> ldc4(const Vec4<double> *p)
+{
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+    const double2 a = q[0], b = q[1];
+    return {a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ void st4(Vec4<float> *p, Vec4<float> v)
+{
+    *reinterpret_cast<float4 *>(p) = make_float4(v.x, v.y, v.z, v.w);
+}
+__device__ __forceinline__ void st4(Vec4<double> *p, Vec4<double> v)
+{
+    double2 *q = reinterpret_cast<double2 *>(p);
+    q[0] = make_double2(v.x, v.y);
+    q[1] = make_double2(v.z, v.w);
+}
+// (q, 1/rho) of a neighbour: the upper half of its aux record
+__device__ __forceinline__ void ld_qinv(const Vec4<float> *p, float &q, float &inv)
+{
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(p) + 1);
+    q = v.x;
+    inv = v.y;
+}
+__device__ __forceinline__ void ld_qinv(const Vec4<double> *p, double &q, double &inv)
+{
+    const double2 v = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+    q = v.x;
+    inv = v.y;
+}
+
+// .w fields carry 32-bit integers (scene index in positions, particle id in velocities)
+__device__ __forceinline__ uint32_t wbits(float w) { return __float_as_uint(w); }
+__device__ __forceinline__ uint32_t wbits(double w) { return (uint32_t) __double_as_longlong(w); }
+template <class R>
+__device__ __forceinline__ R mkw(uint32_t v);
+template <>
+__device__ __forceinline__ float mkw<float>(uint32_t v) { return __uint_as_float(v); }
+template <>
+__device__ __forceinline__ double mkw<double>(uint32_t v) { return __longlong_as_double((long long) v); }
+
+// correctly rounded operations that the compiler may not fuse: the per-particle epilogue
+// mirrors the reference's float expression order
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float inv_sqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double inv_sqrt(double x) { return 1.0 / sqrt(x); }
+
+template <class R>
+__device__ __forceinline__ uint32_t hash_cell(const SceneDev &sc, R x, R y, R z, const Consts<R> &c, int &cx,
+                                              int &cy, int &cz)
+{
+    cx = cell_axis(x, sc.half[0], c.inv_h_f, c.h_d, sc.res[0]);
+    cy = cell_axis(y, sc.half[1], c.inv_h_f, c.h_d, sc.res[1]);
+    cz = cell_axis(z, sc.half[2], c.inv_h_f, c.h_d, sc.res[2]);
+    return sc.cell_base + (uint32_t) cx + (uint32_t) cy * (uint32_t) sc.res[0] +
+           (uint32_t) cz * (uint32_t) sc.res[0] * (uint32_t) sc.res[1];
+}
+
+__device__ __forceinline__ SceneDev load_scene(const SceneDev *scenes, uint32_t s)
+{
+    SceneDev sc;
+    const uint4 *src = reinterpret_cast<const uint4 *>(scenes + s);
+    uint4 *dst = reinterpret_cast<uint4 *>(&sc);
+#pragma unroll
+    for (int k = 0; k < (int) (sizeof(SceneDev) / 16); k++) dst[k] = __ldg(src + k);
+    return sc;
+}
+
+// ------------------------------------------------------------------------------------
+// ingest: host-staged float xyz/vel -> *_u records with scene/id bits, plus the hash.
+// Replaces addParticle + the first H2D of updateGrid; ids follow upload order.
+template <class R>
+__global__ void __launch_bounds__(256) k_ingest(Vec4<R> *__restrict__ pos_u, Vec4<R> *__restrict__ vel_u,
+                                                uint2 *__restrict__ cid_u, uint32_t *__restrict__ count,
+                                                const SceneDev *__restrict__ scenes,
+                                                const uint32_t *__restrict__ scene_off, uint32_t nscenes,
+                                                const float *__restrict__ xyz, const float *__restrict__ vel,
+                                                uint32_t first, uint32_t n, int32_t fixed_scene, uint32_t id0,
+                                                Consts<R> c)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t s, id;
+    if (fixed_scene >= 0) {
+        s = (uint32_t) fixed_scene;
+        id = id0 + k;
+    } else {
+        uint32_t lo = 0, hi = nscenes;  // largest s with scene_off[s] <= k
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(scene_off + mid) <= k) lo = mid;
+            else hi = mid;
+        }
+        s = lo;
+        id = k - __ldg(scene_off + s);
+    }
+    const SceneDev sc = load_scene(scenes, s);
+    const R x = (R) xyz[3 * k], y = (R) xyz[3 * k + 1], z = (R) xyz[3 * k + 2];
+    R vx = 0, vy = 0, vz = 0;
+    if (vel) {
+        vx = (R) vel[3 * k];
+        vy = (R) vel[3 * k + 1];
+        vz = (R) vel[3 * k + 2];
+    }
+    int cx, cy, cz;
+    const uint32_t cell = hash_cell<R>(sc, x, y, z, c, cx, cy, cz);
+    atomicAdd(count + cell, 1u);
+    const uint32_t i = first + k;
+    st4(pos_u + i, Vec4<R>{x, y, z, mkw<R>(s)});
+    st4(vel_u + i, Vec4<R>{vx, vy, vz, mkw<R>(id)});
+    cid_u[i] = make_uint2(cell, id);
+}
+
+// ------------------------------------------------------------------------------------
+// Exclusive scan of the per-cell counts into cell starts (reduce, top-level scan, apply).
+// Replaces scan_local / increment_local_scans (resources/kernels/sph_grid.cl:71-121, 9-23)
+// and its sums-buffer race. The apply phase also seeds the slot cursors and zeroes the
+// counts for the next hash.
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_PER = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &total)
+{
+    __shared__ uint32_t warp_tot[SCAN_THREADS / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t t = lane < (SCAN_THREADS / 32) ? warp_tot[lane] : 0;
+        uint32_t u = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, u, o);
+            if (lane >= o) u += y;
+        }
+        if (lane < (SCAN_THREADS / 32)) warp_tot[lane] = u - t;  // exclusive warp offsets
+    }
+    __syncthreads();
+    const uint32_t excl = warp_tot[wid] + x - v;
+    // block total: last warp's exclusive offset + its inclusive sum
+    __shared__ uint32_t tot;
+    if (threadIdx.x == SCAN_THREADS - 1) tot = excl + v;
+    __syncthreads();
+    total = tot;
+    __syncthreads();
+    return excl;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *__restrict__ count, uint32_t ncells,
+                                                              uint32_t *__restrict__ bsum)
+{
+    const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_PER; k++)
+        if (base + k < ncells) s += count[base + k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ uint32_t w[SCAN_THREADS / 32];
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t t = threadIdx.x < SCAN_THREADS / 32 ? w[threadIdx.x] : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) bsum[blockIdx.x] = t;
+    }
+}
+
+// one block: exclusive scan of the block sums (any count, in chunks), total -> start[ncells]
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_top(uint32_t *__restrict__ bsum, uint32_t nb,
+                                                           uint32_t *__restrict__ start, uint32_t ncells)
+{
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < nb; base += SCAN_THREADS) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = i < nb ? bsum[i] : 0;
+        uint32_t total;
+        const uint32_t e = block_exclusive_scan(v, total);
+        if (i < nb) bsum[i] = carry + e;
+        carry += total;
+    }
+    if (threadIdx.x == 0) start[ncells] = carry;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t *__restrict__ count, uint32_t ncells,
+                                                             const uint32_t *__restrict__ bsum,
+                                                             uint32_t *__restrict__ start,
+                                                             uint32_t *__restrict__ cursor)
+{
+    const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
+    uint32_t v[SCAN_PER];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_PER; k++) {
+        v[k] = base + k < ncells ? count[base + k] : 0;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(s, total) + bsum[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < SCAN_PER; k++) {
+        if (base + k < ncells) {
+            start[base + k] = run;
+            cursor[base + k] = run;
+            count[base + k] = 0;
+        }
+        run += v[k];
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Canonical counting sort: every particle takes a slot in its cell (arbitrary order),
+// then its final position is the cell start plus the number of same-cell particles with
+// a smaller id. The resulting order is ascending (cell, id) regardless of atomic order;
+// the reference leaves the within-cell order unspecified (host std::sort,
+// src/CGPUParticleSimulator.cpp:116-139; swap-remove lists, src/CCPUParticleSimulator.cpp:72-84).
+__global__ void __launch_bounds__(256) k_slot(const uint2 *__restrict__ cid_u, uint32_t n,
+                                              uint32_t *__restrict__ cursor, uint32_t *__restrict__ tmp)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint2 cd = cid_u[i];
+    const uint32_t p = atomicAdd(cursor + cd.x, 1u);
+    tmp[p] = cd.y;
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) k_rank_permute(const uint2 *__restrict__ cid_u, uint32_t n,
+                                                      const uint32_t *__restrict__ start,
+                                                      const uint32_t *__restrict__ tmp,
+                                                      const Vec4<R> *__restrict__ pos_u,
+                                                      const Vec4<R> *__restrict__ vel_u,
+                                                      Vec4<R> *__restrict__ pos_s, Vec4<R> *__restrict__ vel_s)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint2 cd = cid_u[i];
+    const uint32_t b = start[cd.x], e = start[cd.x + 1];
+    uint32_t r = 0;
+    for (uint32_t k = b; k < e; k++) r += tmp[k] < cd.y ? 1u : 0u;
+    const uint32_t dst = b + r;
+    st4(pos_s + dst, ld4(pos_u + i));
+    st4(vel_s + dst, ld4(vel_u + i));
+}
+
+// ------------------------------------------------------------------------------------
+// Neighbour walk: the 27 cells around a particle are 9 rows (dy, dz) of 3 cells along x,
+// and in (cell, id) order each row is one contiguous range of the sorted arrays.
+template <class R, class F>
+__device__ __forceinline__ void for_each_row(const SceneDev &sc, const uint32_t *__restrict__ start, int cx, int cy,
+                                             int cz, F &&f)
+{
+    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
+    const int xl = cx > 0 ? cx - 1 : 0;
+    const int xh = cx + 1 < X ? cx + 1 : X - 1;
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; dz++) {
+        const int z = cz + dz;
+        if (z < 0 || z >= Z) continue;
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; dy++) {
+            const int y = cy + dy;
+            if (y < 0 || y >= Y) continue;
+            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
+            const uint32_t jb = __ldg(start + row + xl);
+            const uint32_t je = __ldg(start + row + xh + 1);
+            f(jb, je);
+        }
+    }
+}
+
+// Density and pressure (src/CCPUParticleSimulator.cpp:93-141): rho = m * poly6 * sum (h^2-r^2)^3
+// over r^2 <= h^2, self included; p = k (rho - rho0). Also stores p / rho^2 and 1 / rho,
+// the two per-neighbour factors of the force pass.
+template <class R>
+__global__ void __launch_bounds__(256) k_density(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
+                                                 const uint32_t *__restrict__ start,
+                                                 const SceneDev *__restrict__ scenes, uint32_t n, Consts<R> c)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Vec4<R> pi = ld4(pos + i);
+    const SceneDev sc = load_scene(scenes, wbits(pi.w));
+    int cx, cy, cz;
+    hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
+    R acc = 0;
+    const R h2 = c.h2;
+    for_each_row<R>(sc, start, cx, cy, cz, [&](uint32_t jb, uint32_t je) {
+#pragma unroll 4
+        for (uint32_t j = jb; j < je; j++) {
+            const Vec4<R> pj = ld4(pos + j);
+            const R dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            const R r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 <= h2) {
+                const R t = h2 - r2;
+                acc += t * t * t;
+            }
+        }
+    });
+    const R rho = rmul(rmul(acc, c.c_poly6), c.mass);
+    const R p = rmul(c.k, rsub(rho, c.rho0));
+    st4(aux + i, Vec4<R>{rho, p, rdiv(p, rmul(rho, rho)), rdiv((R) 1, rho)});
+}
+
+// Forces (src/CCPUParticleSimulator.cpp:143-203), walls (src/CCollisionGeometry.cpp:117-133),
+// obstacles, position-Verlet integration (src/CCPUParticleSimulator.cpp:211-229) and the
+// cell hash of the new position for the next step, in one pass.
+template <class R>
+__global__ void __launch_bounds__(256) k_forces(const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel,
+                                                const Vec4<R> *__restrict__ aux, const uint32_t *__restrict__ start,
+                                                const SceneDev *__restrict__ scenes,
+                                                const ObstacleDev *__restrict__ obstacles, uint32_t n, Consts<R> c,
+                                                Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out,
+                                                Vec4<R> *__restrict__ acc_out, uint2 *__restrict__ cid_out,
+                                                uint32_t *__restrict__ count)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Vec4<R> pi = ld4(pos + i);
+    const Vec4<R> vi = ld4(vel + i);
+    const Vec4<R> ai = ld4(aux + i);
+    const uint32_t s = wbits(pi.w), id = wbits(vi.w);
+    const SceneDev sc = load_scene(scenes, s);
+    int cx, cy, cz;
+    hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
+    const R h = c.h, h2 = c.h2, qi = ai.z;
+    R fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
+    for_each_row<R>(sc, start, cx, cy, cz, [&](uint32_t jb, uint32_t je) {
+#pragma unroll 2
+        for (uint32_t j = jb; j < je; j++) {
+            const Vec4<R> pj = ld4(pos + j);
+            const R dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            const R r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 <= h2 && j != i) {
+                const Vec4<R> vj = ld4(vel + j);
+                R qj, invj;
+                ld_qinv(aux + j, qj, invj);
+                const R rinv = inv_sqrt(r2);
+                const R hr = h - r2 * rinv;
+                const R w = (qi + qj) * (c.c_spiky * hr * hr * rinv);  // (p_i/rho_i^2 + p_j/rho_j^2) grad W
+                fpx += w * dx;
+                fpy += w * dy;
+                fpz += w * dz;
+                const R l = c.c_visc * hr * invj;                      // lap W / rho_j
+                fvx += (vj.x - vi.x) * l;
+                fvy += (vj.y - vi.y) * l;
+                fvz += (vj.z - vi.z) * l;
+            }
+        }
+    });
+    const R rho = ai.x;
+    const R sp = rmul(-c.mass, rho), sv = rmul(c.mu, c.mass);
+    R ax = rdiv(radd(radd(rmul(fpx, sp), rmul(fvx, sv)), rmul((R) sc.gravity[0], rho)), rho);
+    R ay = rdiv(radd(radd(rmul(fpy, sp), rmul(fvy, sv)), rmul((R) sc.gravity[1], rho)), rho);
+    R az = rdiv(radd(radd(rmul(fpz, sp), rmul(fvz, sv)), rmul((R) sc.gravity[2], rho)), rho);
+
+    // walls at -+box/2 in the order left, bottom, back, right, top, front; the inverse
+    // normal of wall w points into the box along axis w % 3
+    R wx = 0, wy = 0, wz = 0;
+    const R p3[3] = {pi.x, pi.y, pi.z};
+    const R v3[3] = {vi.x, vi.y, vi.z};
+#pragma unroll
+    for (int w = 0; w < 6; w++) {
+        const int a = w % 3;
+        const R sgn = w < 3 ? (R) 1 : (R) -1;                   // inverse normal component
+        const R wallp = w < 3 ? -(R) sc.half[a] : (R) sc.half[a];
+        const R d = radd(rmul(rsub(wallp, p3[a]), sgn), c.wall_r);
+        if (d > (R) 0) {
+            const R kt = rmul(rmul(sgn, c.wall_k), d);
+            const R dt = rmul(sgn, rmul(c.wall_damp, rmul(v3[a], sgn)));
+            if (a == 0) { wx = radd(radd(wx, kt), dt); }
+            else if (a == 1) { wy = radd(radd(wy, kt), dt); }
+            else { wz = radd(radd(wz, kt), dt); }
+        }
+    }
+    // box obstacles: inside the obstacle grown by the particle radius, push out through the
+    // nearest face with the wall spring and damping
+    for (uint32_t o = 0; o < sc.n_obs; o++) {
+        const ObstacleDev ob = obstacles[sc.obs_base + o];
+        R best = (R) 1e30;
+        int bf = -1;
+#pragma unroll
+        for (int f = 0; f < 6; f++) {
+            const int a = f % 3;
+            const R dpen = f < 3 ? radd(rsub(p3[a], (R) ob.lo[a]), c.wall_r) : radd(rsub((R) ob.hi[a], p3[a]), c.wall_r);
+            if (dpen <= (R) 0) { bf = -2; }
+            if (bf != -2 && dpen < best) { best = dpen; bf = f; }
+        }
+        if (bf >= 0) {
+            const int a = bf % 3;
+            const R sgn = bf < 3 ? (R) -1 : (R) 1;  // outward normal of the face
+            const R kt = rmul(rmul(sgn, c.wall_k), best);
+            const R dt = rmul(sgn, rmul(c.wall_damp, rmul(v3[a], sgn)));
+            if (a == 0) { wx = radd(radd(wx, kt), dt); }
+            else if (a == 1) { wy = radd(radd(wy, kt), dt); }
+            else { wz = radd(radd(wz, kt), dt); }
+        }
+    }
+    ax = radd(ax, wx);
+    ay = radd(ay, wy);
+    az = radd(az, wz);
+
+    // x' = x + v dt + (a dt) dt ; v' = (x' - x) / dt
+    const R dt = c.dt;
+    const R nx = radd(radd(pi.x, rmul(vi.x, dt)), rmul(rmul(ax, dt), dt));
+    const R ny = radd(radd(pi.y, rmul(vi.y, dt)), rmul(rmul(ay, dt), dt));
+    const R nz = radd(radd(pi.z, rmul(vi.z, dt)), rmul(rmul(az, dt), dt));
+    const R nvx = rdiv(rsub(nx, pi.x), dt), nvy = rdiv(rsub(ny, pi.y), dt), nvz = rdiv(rsub(nz, pi.z), dt);
+    st4(pos_out + i, Vec4<R>{nx, ny, nz, pi.w});
+    st4(vel_out + i, Vec4<R>{nvx, nvy, nvz, vi.w});
+    if (acc_out) st4(acc_out + i, Vec4<R>{ax, ay, az, (R) 0});
+    int qx, qy, qz;
+    const uint32_t cell = hash_cell<R>(sc, nx, ny, nz, c, qx, qy, qz);
+    atomicAdd(count + cell, 1u);
+    cid_out[i] = make_uint2(cell, id);
+}
+
+// ------------------------------------------------------------------------------------
+// egress: any layout -> id-ordered, scene-major staging arrays for one D2H copy each.
+template <class R>
+__global__ void __launch_bounds__(256) k_egress(const Vec4<R> *__restrict__ posL, const Vec4<R> *__restrict__ velL,
+                                                const Vec4<R> *__restrict__ posA, const Vec4<R> *__restrict__ velA,
+                                                const Vec4<R> *__restrict__ aux, const Vec4<R> *__restrict__ pos_u,
+                                                const Vec4<R> *__restrict__ vel_u, const Vec4<R> *__restrict__ acc,
+                                                const uint32_t *__restrict__ scene_off, uint32_t n_state,
+                                                uint32_t n_aux, uint32_t n_acc, R *xyz, R *v, R *rho, R *p, R *a)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_state) {
+        const Vec4<R> pp = ldc4(posL + i), vv = ldc4(velL + i);
+        const uint32_t o = __ldg(scene_off + wbits(pp.w)) + wbits(vv.w);
+        xyz[3 * o] = pp.x; xyz[3 * o + 1] = pp.y; xyz[3 * o + 2] = pp.z;
+        v[3 * o] = vv.x; v[3 * o + 1] = vv.y; v[3 * o + 2] = vv.z;
+    }
+    if (i < n_aux) {
+        const Vec4<R> pp = ldc4(posA + i), vv = ldc4(velA + i);
+        const uint32_t o = __ldg(scene_off + wbits(pp.w)) + wbits(vv.w);
+        const Vec4<R> ax = ldc4(aux + i);
+        rho[o] = ax.x;
+        p[o] = ax.y;
+    }
+    if (acc && i < n_acc) {
+        const Vec4<R> pp = ldc4(pos_u + i), vv = ldc4(vel_u + i);
+        const uint32_t o = __ldg(scene_off + wbits(pp.w)) + wbits(vv.w);
+        const Vec4<R> aa = ldc4(acc + i);
+        a[3 * o] = aa.x; a[3 * o + 1] = aa.y; a[3 * o + 2] = aa.z;
+    }
+}
+
+// FP64 reductions per scene, one block per scene over the scene's contiguous range, fixed
+// reduction order (deterministic): mass, momentum, kinetic energy, mean and max density.
+template <class R>
+__global__ void __launch_bounds__(256) k_stats(const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
+                                               const uint32_t *__restrict__ start,
+                                               const SceneDev *__restrict__ scenes, double mass,
+                                               double *__restrict__ out)
+{
+    const SceneDev sc = load_scene(scenes, blockIdx.x);
+    const uint32_t b = start[sc.cell_base], e = start[sc.cell_base + sc.ncells];
+    double mx = 0, my = 0, mz = 0, ke = 0, rs = 0, rmax = -1e300;
+    for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        const Vec4<R> v = ldc4(vel + i);
+        const Vec4<R> a = ldc4(aux + i);
+        const double vx = (double) v.x, vy = (double) v.y, vz = (double) v.z;
+        mx += vx; my += vy; mz += vz;
+        ke += vx * vx + vy * vy + vz * vz;
+        rs += (double) a.x;
+        rmax = fmax(rmax, (double) a.x);
+    }
+    __shared__ double red[6][256];
+    red[0][threadIdx.x] = mx; red[1][threadIdx.x] = my; red[2][threadIdx.x] = mz;
+    red[3][threadIdx.x] = ke; red[4][threadIdx.x] = rs; red[5][threadIdx.x] = rmax;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int) threadIdx.x < w) {
+#pragma unroll
+            for (int k = 0; k < 5; k++) red[k][threadIdx.x] += red[k][threadIdx.x + w];
+            red[5][threadIdx.x] = fmax(red[5][threadIdx.x], red[5][threadIdx.x + w]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double cnt = (double) (e - b);
+        double *o = out + 8 * blockIdx.x;
+        o[0] = mass * cnt;
+        o[1] = mass * red[0][0]; o[2] = mass * red[1][0]; o[3] = mass * red[2][0];
+        o[4] = 0.5 * mass * red[3][0];
+        o[5] = cnt > 0 ? red[4][0] / cnt : 0.0;
+        o[6] = cnt > 0 ? red[5][0] : 0.0;
+        o[7] = cnt;
+    }
+}
+
+// ------------------------------------------------------------------------------------
+static inline unsigned nblk(uint32_t n, unsigned t) { return (unsigned) ((n + t - 1) / t); }
+
+template <class R>
+cudaError_t Launch<R>::ingest(const DevBufs &b, const float *xyz, const float *vel, uint32_t first, uint32_t n,
+                              int32_t scene, uint32_t id0, uint32_t nscenes, Consts<R> c, cudaStream_t st)
+{
+    if (!n) return cudaSuccess;
+    k_ingest<R><<<nblk(n, 256), 256, 0, st>>>((Vec4<R> *) b.pos_u, (Vec4<R> *) b.vel_u, b.cid_u, b.count, b.scenes,
+                                              b.scene_off, nscenes, xyz, vel, first, n, scene, id0, c);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t Launch<R>::scan(const DevBufs &b, uint32_t ncells, cudaStream_t st)
+{
+    const uint32_t nb = (ncells + SCAN_TILE - 1) / SCAN_TILE;
+    k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum);
+    k_scan_top<<<1, SCAN_THREADS, 0, st>>>(b.bsum, nb, b.start, ncells);
+    k_scan_apply<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, b.start, b.cursor);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t Launch<R>::permute(const DevBufs &b, uint32_t n, cudaStream_t st)
+{
+    if (!n) return cudaSuccess;
+    k_slot<<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.cursor, b.tmp);
+    k_rank_permute<R><<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.start, b.tmp, (const Vec4<R> *) b.pos_u,
+                                                    (const Vec4<R> *) b.vel_u, (Vec4<R> *) b.pos_s,
+                                                    (Vec4<R> *) b.vel_s);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t Launch<R>::density(const DevBufs &b, uint32_t n, Consts<R> c, cudaStream_t st)
+{
+    if (!n) return cudaSuccess;
+    k_density<R><<<nblk(n, 256), 256, 0, st>>>((const Vec4<R> *) b.pos_s, (Vec4<R> *) b.aux, b.start, b.scenes, n, c);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool record_acc, cudaStream_t st)
+{
+    if (!n) return cudaSuccess;
+    k_forces<R><<<nblk(n, 256), 256, 0, st>>>((const Vec4<R> *) b.pos_s, (const Vec4<R> *) b.vel_s,
+                                              (const Vec4<R> *) b.aux, b.start, b.scenes, b.obstacles, n, c,
+                                              (Vec4<R> *) b.pos_u, (Vec4<R> *) b.vel_u,
+                                              record_acc ? (Vec4<R> *) b.acc : nullptr, b.cid_u, b.count);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t Launch<R>::egress(const DevBufs &b, uint32_t n_state, uint32_t n_aux, uint32_t n_acc, int layout_sorted,
+                              int aux_sorted, cudaStream_t st)
+{
+    if (!n_state) return cudaSuccess;
+    const Vec4<R> *posL = (const Vec4<R> *) (layout_sorted ? b.pos_s : b.pos_u);
+    const Vec4<R> *velL = (const Vec4<R> *) (layout_sorted ? b.vel_s : b.vel_u);
+    const Vec4<R> *posA = (const Vec4<R> *) (aux_sorted ? b.pos_s : b.pos_u);
+    const Vec4<R> *velA = (const Vec4<R> *) (aux_sorted ? b.vel_s : b.vel_u);
+    R *xyz, *v, *rho, *p, *a;
+    if (sizeof(R) == 8) {
+        xyz = (R *) b.st_xyz64; v = (R *) b.st_vel64; rho = (R *) b.st_rho64; p = (R *) b.st_p64; a = (R *) b.st_acc64;
+    } else {
+        xyz = (R *) b.st_xyz; v = (R *) b.st_vel; rho = (R *) b.st_rho; p = (R *) b.st_p; a = (R *) b.st_acc;
+    }
+    k_egress<R><<<nblk(n_state, 256), 256, 0, st>>>(posL, velL, posA, velA, (const Vec4<R> *) b.aux,
+                                                    (const Vec4<R> *) b.pos_u, (const Vec4<R> *) b.vel_u,
+                                                    a ? (const Vec4<R> *) b.acc : nullptr, b.scene_off, n_state,
+                                                    n_aux, n_acc, xyz, v, rho, p, a);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t Launch<R>::stats(const DevBufs &b, uint32_t nscenes, Consts<R> c, int layout_sorted, cudaStream_t st)
+{
+    const Vec4<R> *vel = (const Vec4<R> *) (layout_sorted ? b.vel_s : b.vel_u);
+    k_stats<R><<<nscenes, 256, 0, st>>>(vel, (const Vec4<R> *) b.aux, b.start, b.scenes, (double) c.mass, b.stats);
+    return cudaGetLastError();
+}
+
+template struct Launch<float>;
+template struct Launch<double>;
+
+}  // namespace sph

@@ -1,0 +1,193 @@
+/*
+ * sph_cuda.h -- C ABI of the GB300 (sm_103a) SPH grid step.
+ *
+ * This is the drop-in boundary for the uniform-grid SPH step that the reference's
+ * CGPUParticleSimulator runs (src/CGPUParticleSimulator.cpp:57-173 with
+ * src/CGPUBaseParticleSimulator.cpp:59-97). A CBaseParticleSimulator subclass
+ * (include/CBaseParticleSimulator.h:29-110) calls these functions in place of the
+ * OpenCL wrapper and kernels. Plain C types only: host pointers, sizes, status codes.
+ *
+ * Conventions
+ *  - Every function returning int returns SPH_OK (0) or a negative SPH_ERR_* code and
+ *    never throws; the message of the last failure is sph_last_error(ctx). This replaces
+ *    the reference's CLException (src/CLWrapper.cpp:115-121) that
+ *    CGPUBaseParticleSimulator::step catches (src/CGPUBaseParticleSimulator.cpp:28-37).
+ *  - One context belongs to one host thread at a time; it owns one CUDA stream on one
+ *    device. Calls are stream-ordered; download/stat functions synchronise that stream.
+ *  - Arrays of particles are scene-major and, within a scene, in id order (ids are
+ *    0..n-1 in upload order, then appended particles), float xyz triples.
+ *  - A context holds 1..n independent scenes (a batch); every pass covers all scenes
+ *    in one launch.
+ */
+#ifndef SPH_CUDA_H
+#define SPH_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_OK 0
+#define SPH_ERR_ARG (-1)         /* invalid argument */
+#define SPH_ERR_CUDA (-2)        /* CUDA runtime or launch error */
+#define SPH_ERR_CAPACITY (-3)    /* more particles than the scene's capacity */
+#define SPH_ERR_STATE (-4)       /* call out of order (e.g. step before upload) */
+#define SPH_ERR_NOMEM (-5)       /* device or host allocation failed */
+#define SPH_ERR_UNSUPPORTED (-6) /* option not available in this build */
+#define SPH_ERR_DEVICE (-7)      /* a kernel reported an error status */
+
+/* Arithmetic of the step. */
+#define SPH_PLAIN_F32 0 /* all-FP32 state and arithmetic */
+#define SPH_F64 1       /* the same method in FP64 (reference run) */
+#define SPH_MIXED 2     /* 16-bit cell-relative positions, FP16 velocities, Kahan densities */
+
+/* sph_params.flags */
+#define SPH_FLAG_PROFILE 1u    /* record per-pass CUDA-event times (sph_pass_times) */
+#define SPH_FLAG_RECORD_ACC 2u /* keep each step's accelerations for sph_download */
+
+typedef struct sph_ctx sph_ctx;
+
+/* Physical and numerical parameters; sph_params_default fills the reference's values:
+ * h, mass, gas stiffness, rest density, viscosity from include/CParticle.h:80-84;
+ * dt = 0.01 from src/CBaseParticleSimulator.cpp:7; gravity (0, -9.80665, 0) from
+ * include/CBaseParticleSimulator.h:19; wall constants 10000 / -0.9 from
+ * include/CCollisionGeometry.h:20-21 and the 0.01 particle radius of
+ * src/CCollisionGeometry.cpp:124. */
+typedef struct sph_params {
+    uint32_t struct_size; /* sizeof(sph_params) */
+    float h;
+    float mass;
+    float gas_stiffness;
+    float rest_density;
+    float viscosity;
+    float dt;
+    float gravity[3];
+    float wall_k;
+    float wall_damping;
+    float wall_radius;
+    int32_t precision; /* SPH_PLAIN_F32, SPH_F64 or SPH_MIXED */
+    uint32_t flags;    /* SPH_FLAG_* */
+    int32_t device;    /* CUDA device ordinal */
+} sph_params;
+
+/* One scene of a batch: an axis-aligned box centred on the origin (walls at +-box/2,
+ * as CCollisionGeometry builds them from the grid cuboid), a particle capacity, and
+ * optional axis-aligned box obstacles (min xyz then max xyz, 6 floats each) that push
+ * particles out with the wall spring and damping constants. */
+typedef struct sph_scene_desc {
+    float box[3];
+    uint32_t max_particles;
+    uint32_t n_obstacles;
+    const float *obstacles; /* 6 * n_obstacles floats, may be NULL when n_obstacles == 0 */
+} sph_scene_desc;
+
+/* Fills the reference's constants (see sph_params). */
+void sph_params_default(sph_params *p);
+
+/* One scene; replaces the CGPUParticleSimulator constructor + setupKernels
+ * (src/CGPUParticleSimulator.cpp:3-55). box: 3 extents (the reference's scalar boxSize
+ * is box = {s, s, s}). */
+int sph_create(const sph_params *p, const float box[3], uint32_t max_particles, sph_ctx **out);
+
+/* n_scenes independent scenes stepped together (no reference counterpart; one launch
+ * per pass over all scenes). */
+int sph_batch_create(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *scenes, sph_ctx **out);
+
+void sph_destroy(sph_ctx *ctx);
+
+/* Last error message of ctx (or of the last failed create when ctx is NULL). */
+const char *sph_last_error(const sph_ctx *ctx);
+
+/* Replaces CGPUBaseParticleSimulator::getSelectedDevice (src/CGPUBaseParticleSimulator.cpp:17-20). */
+const char *sph_device_name(const sph_ctx *ctx);
+
+/* The CUDA stream (a cudaStream_t) every call of ctx launches on, for callers that order
+ * their own work or record their own events against the step (no reference counterpart:
+ * CLWrapper keeps its command queue private, src/CLWrapper.cpp:3-13). */
+void *sph_stream(const sph_ctx *ctx);
+
+/* Replaces every scene's particles: counts[s] particles for scene s, concatenated
+ * scene-major; vel may be NULL (zero). Ids restart at 0 in each scene. Mirrors
+ * setupScene's addParticle loop (src/CBaseParticleSimulator.cpp:38-74) followed by the
+ * first H2D copy of CGPUParticleSimulator::updateGrid (src/CGPUParticleSimulator.cpp:59). */
+int sph_upload(sph_ctx *ctx, const float *xyz, const float *vel, const uint32_t *counts);
+
+/* Appends n particles to one scene (emitters, e.g. the FOUNTAIN scenario's
+ * generateParticles, src/CBaseParticleSimulator.cpp:187-210). */
+int sph_append(sph_ctx *ctx, uint32_t scene, const float *xyz, const float *vel, uint32_t n);
+
+/* CGPUBaseParticleSimulator::setGravityVector (src/CGPUBaseParticleSimulator.cpp:11-15).
+ * scene < 0 sets every scene. */
+int sph_set_gravity(sph_ctx *ctx, int32_t scene, const float g[3]);
+
+/* nsteps steps of CBaseParticleSimulator::step (src/CBaseParticleSimulator.cpp:116-144):
+ * grid build, density/pressure, forces + walls + integration, all on the device. */
+int sph_step(sph_ctx *ctx, int32_t nsteps);
+
+/* The three device passes of one step, for the reference's pass-by-pass interface
+ * (include/CBaseParticleSimulator.h:92-96): updateGrid (src/CGPUParticleSimulator.cpp:57-139),
+ * updateDensityPressure (:141-155), and updateForces (:157-173) fused with
+ * updateCollisions and integrate (src/CGPUBaseParticleSimulator.cpp:59-97).
+ * Must be called in this order. */
+int sph_pass_grid(sph_ctx *ctx);
+int sph_pass_density(sph_ctx *ctx);
+int sph_pass_forces(sph_ctx *ctx);
+
+/* Milliseconds of the last step's passes (grid, density, forces, collisions, integrate),
+ * the fields of sProfilingEvent (include/SProfilingEvent.h:8-31). Needs SPH_FLAG_PROFILE;
+ * collisions and integrate are fused into forces and report 0. */
+int sph_pass_times(sph_ctx *ctx, double ms[5]);
+
+/* Particle count of every scene (n_scenes entries). */
+int sph_get_counts(const sph_ctx *ctx, uint32_t *counts);
+uint32_t sph_num_scenes(const sph_ctx *ctx);
+uint64_t sph_num_particles(const sph_ctx *ctx);
+/* Grid resolution of one scene: (int) ceil(box / h) per axis (src/CBaseParticleSimulator.cpp:27-31). */
+int sph_get_resolution(const sph_ctx *ctx, uint32_t scene, int32_t res[3]);
+
+/* State after the last call, scene-major and in id order. Any pointer may be NULL.
+ * rho / p are the densities and pressures of the last density pass; acc needs
+ * SPH_FLAG_RECORD_ACC. Replaces the readback of CGPUBaseParticleSimulator::integrate
+ * (src/CGPUBaseParticleSimulator.cpp:84-91). */
+int sph_download(sph_ctx *ctx, float *xyz, float *vel, float *rho, float *p, float *acc);
+/* Same in double, for SPH_F64 contexts. */
+int sph_download_f64(sph_ctx *ctx, double *xyz, double *vel, double *rho, double *p, double *acc);
+
+/* The grid of the last grid pass: the cell of every particle (scene-major, id order,
+ * cell index local to its scene: x + y*X + z*X*Y), the count of every cell (scene-major),
+ * and the ids of each scene's particles in sorted order, ascending (cell, id). Any
+ * pointer may be NULL. */
+int sph_get_grid(sph_ctx *ctx, uint32_t *cell_of_particle, uint32_t *cell_counts, uint32_t *sorted_ids);
+
+/* FP64 reductions of one scene over the current state: out[0] mass, out[1..3] momentum,
+ * out[4] kinetic energy, out[5] mean density, out[6] max density, out[7] particle count. */
+int sph_stats(sph_ctx *ctx, uint32_t scene, double out[8]);
+
+/* ---- scene generators (host only, no device needed) ---- */
+
+/* The reference's DAM_BREAK lattice for a cubic box (src/CBaseParticleSimulator.cpp:38-58).
+ * Returns the particle count; writes at most cap particles. */
+int64_t sph_scene_reference_dam_break(float box, float *xyz, uint64_t cap);
+
+/* A dims[0] x dims[1] x dims[2] lattice of the given spacing anchored at the box's min
+ * corner (-box/2), each coordinate jittered by uniform [-jitter, +jitter) * spacing from a
+ * seeded splitmix64 stream; particles ordered y outer, x, z inner like the reference. */
+int sph_scene_lattice(const uint32_t dims[3], const float box[3], float spacing, float jitter, uint64_t seed, float *xyz);
+
+/* Seeded plan of a batch of dam-break scenes: counts log-uniform in [nmin, nmax], aspect
+ * per axis uniform in [amin, amax]; writes lattice dims (3 per scene) and boxes (3 per
+ * scene) that keep the fill fraction of the 20^3-lattice, 1.0 x 1.0 x 0.5 m scene. */
+int sph_scene_batch_plan(uint32_t n_scenes, uint64_t seed, uint32_t nmin, uint32_t nmax, float amin, float amax,
+                         uint32_t *dims, float *boxes);
+
+/* Disc emitter: n particles on a disc of the given radius in the y = center[1] plane,
+ * velocity (0, speed, 0) plus N(0, sigma^2) per component; seeded by (seed, step). */
+int sph_scene_fountain_emit(uint64_t seed, uint32_t step, uint32_t n, const float center[3], float radius, float speed,
+                            float sigma, float *xyz, float *vel);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPH_CUDA_H */

@@ -1,0 +1,348 @@
+"""GPU parity of the CUDA step (through the C ABI) against the oracle.
+
+Tolerances (see helpers.py): plain FP32 within 1e-5 relative to each quantity's scale;
+the FP64 GPU run within 1e-10 of the FP64 oracle; the grid (cells, counts, sorted order)
+bit-exact. Long runs are chaotic, so they are compared as bands on aggregates.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import assert_within, rel_errors
+
+pytestmark = pytest.mark.gpu
+
+H32 = np.float32(0.0457)
+C0_BOX = (1.0, 1.0, 0.5)
+G981 = (0.0, -9.81, 0.0)
+
+
+def c0_scene(sphlib, dims=(20, 20, 20), box=C0_BOX, seed=0):
+    return sphlib.dam_break_scene(dims, box, seed)
+
+
+def gpu_run(sphlib, box, pos, vel=None, steps=1, precision=0, gravity=None, flags=2):
+    ctx = sphlib.SphContext(box, pos.shape[0], precision=precision, flags=flags, gravity=gravity)
+    ctx.upload(pos, vel)
+    ctx.step(steps)
+    out = ctx.download(acc=bool(flags & 2))
+    ctx.close()
+    return out
+
+
+def oracle_run(O, box, pos, vel=None, steps=1, mode=None, gravity=None):
+    o = O.Oracle(box, O.REF if mode is None else mode, threads=os.cpu_count(), gravity=gravity)
+    o.add(pos, vel)
+    o.step(steps)
+    s = o.state64() if mode == O.F64 else o.state()
+    s["ascale"] = o.state()["ascale"]
+    return s
+
+
+def cells_numpy(pos, box):
+    """The reference's hash, vectorised in float64: floor((p + box/2.0) / h), clamped."""
+    box = np.asarray(box, np.float32)
+    res = np.ceil(box / H32).astype(np.int64)
+    q = (pos.astype(np.float64) + box.astype(np.float64) / 2.0) / np.float64(H32)
+    c = np.floor(q)
+    c = np.where(q >= 0, c, 0)
+    c = np.minimum(c, res - 1).astype(np.int64)
+    return c[:, 0] + c[:, 1] * res[0] + c[:, 2] * res[0] * res[1], res
+
+
+def scenes(sphlib, oracle_mod):
+    rng = np.random.default_rng(11)
+    out = {"ref_default_0.4": ((0.4, 0.4, 0.4), oracle_mod.reference_dam_break(0.4), None, None)}
+    p = c0_scene(sphlib)
+    out["c0_8000"] = (C0_BOX, p, None, G981)
+    out["c0_8000_moving"] = (C0_BOX, p, rng.normal(0, 0.5, p.shape).astype(np.float32), G981)
+    q = c0_scene(sphlib, dims=(12, 9, 14), box=(0.45, 0.5, 0.6), seed=5)
+    q[:40] -= np.float32(0.02)  # some outside the min walls: clamped cells, wall forces
+    out["outside_walls"] = ((0.45, 0.5, 0.6), q, rng.normal(0, 0.2, q.shape).astype(np.float32), None)
+    return out
+
+
+# ------------------------------------------------------------------------- grid
+def test_grid_bit_exact(sphlib, oracle_mod):
+    O = oracle_mod
+    for name, (box, pos, vel, g) in scenes(sphlib, oracle_mod).items():
+        ctx = sphlib.SphContext(box, pos.shape[0], gravity=g)
+        ctx.upload(pos, vel)
+        for rep in range(2):
+            cur = ctx.download()["pos"] if rep else pos
+            ctx.pass_grid()
+            cell, counts, order = ctx.grid()
+            o = O.Oracle(box, O.REF, threads=1)
+            o.add(cur)
+            o.update_grid()
+            ocell, ocounts, oorder = o.grid()
+            assert np.array_equal(cell, ocell.astype(np.uint32)), name
+            assert np.array_equal(counts, ocounts.astype(np.uint32)), name
+            assert np.array_equal(order, oorder.astype(np.uint32)), name
+            ncell, _ = cells_numpy(cur, box)
+            assert np.array_equal(cell.astype(np.int64), ncell), name
+            # finish this step and re-check the grid of the moved particles
+            ctx.pass_density()
+            ctx.pass_forces()
+            ctx.step(4)
+        ctx.close()
+
+
+def test_grid_cell_faces(sphlib, oracle_mod):
+    """Coordinates on and one ulp around every cell face hash exactly as the double formula."""
+    box = (0.4, 0.4, 0.4)
+    faces = [np.float32(np.float32(k) * H32 - np.float32(0.2)) for k in range(0, 10)]
+    vals = []
+    for f in faces:
+        vals += [f, np.nextafter(f, np.float32(-1)), np.nextafter(f, np.float32(1))]
+    vals = np.array(vals, np.float32)
+    rng = np.random.default_rng(1)
+    pos = np.stack([vals, rng.permutation(vals), rng.permutation(vals)], axis=1).astype(np.float32)
+    ctx = sphlib.SphContext(box, pos.shape[0])
+    ctx.upload(pos)
+    ctx.pass_grid()
+    cell, counts, order = ctx.grid()
+    want, _ = cells_numpy(pos, box)
+    assert np.array_equal(cell.astype(np.int64), want)
+    o = oracle_mod.Oracle(box, oracle_mod.CANON, threads=1)
+    o.add(pos)
+    o.update_grid()
+    assert np.array_equal(order, o.grid()[2].astype(np.uint32))
+    ctx.close()
+
+
+# ------------------------------------------------------------------------- one step
+@pytest.mark.parametrize("name", ["ref_default_0.4", "c0_8000", "c0_8000_moving", "outside_walls"])
+def test_one_step_plain_vs_oracle(sphlib, oracle_mod, name):
+    box, pos, vel, g = scenes(sphlib, oracle_mod)[name]
+    got = gpu_run(sphlib, box, pos, vel, gravity=g)
+    ref = oracle_run(oracle_mod, box, pos, vel, gravity=g)
+    assert_within(rel_errors(got, ref), name)
+
+
+@pytest.mark.parametrize("name", ["ref_default_0.4", "c0_8000_moving", "outside_walls"])
+def test_one_step_f64_vs_oracle_f64(sphlib, oracle_mod, name):
+    O = oracle_mod
+    box, pos, vel, g = scenes(sphlib, oracle_mod)[name]
+    got = gpu_run(sphlib, box, pos, vel, gravity=g, precision=sphlib.SPH_F64)
+    ref = oracle_run(O, box, pos, vel, gravity=g, mode=O.F64)
+    assert np.max(np.abs(got["rho"] - ref["rho"]) / ref["rho"]) < 1e-12
+    err = np.linalg.norm(got["acc"] - ref["acc"], axis=1) / ref["ascale"]
+    assert err.max() < 1e-10
+    assert np.abs(got["pos"] - ref["pos"]).max() < 1e-13
+
+
+@pytest.mark.parametrize("name", ["ref_default_0.4", "c0_8000_moving"])
+def test_one_step_plain_vs_f64_gpu(sphlib, oracle_mod, name):
+    box, pos, vel, g = scenes(sphlib, oracle_mod)[name]
+    a = gpu_run(sphlib, box, pos, vel, gravity=g)
+    b = gpu_run(sphlib, box, pos, vel, gravity=g, precision=sphlib.SPH_F64)
+    b["ascale"] = oracle_run(oracle_mod, box, pos, vel, gravity=g, mode=oracle_mod.F64)["ascale"]
+    assert_within(rel_errors(a, b), name)
+
+
+def _golden():
+    with open(os.path.join(os.path.dirname(__file__), "golden", "analytic_cases.json")) as f:
+        return json.load(f)["cases"]
+
+
+@pytest.mark.parametrize("case", _golden(), ids=lambda c: c["name"])
+def test_golden_cases_on_gpu(sphlib, case):
+    pos = np.array(case["pos"], np.float32)
+    vel = np.array(case["vel"], np.float32)
+    got = gpu_run(sphlib, case["box"], pos, vel, gravity=case["gravity"])
+    ref = {"rho": np.array(case["rho"]), "p": np.array(case["p"]), "acc": np.array(case["acc"]),
+           "ascale": np.array(case["acc_scale"]), "pos": np.array(case["pos_new"]),
+           "vel": np.array(case["vel_new"])}
+    assert_within(rel_errors(got, ref), case["name"])
+    g64 = gpu_run(sphlib, case["box"], pos, vel, gravity=case["gravity"], precision=sphlib.SPH_F64)
+    np.testing.assert_allclose(g64["rho"], case["rho"], rtol=1e-12)
+    err = np.linalg.norm(g64["acc"] - np.array(case["acc"]), axis=1) / np.array(case["acc_scale"])
+    assert err.max() < 1e-11
+
+
+# ------------------------------------------------------------------------- long runs
+def test_bands_vs_f64_c0(sphlib):
+    """8,000-particle dam break, 200 steps: per-step mean/max density, kinetic energy and mass
+    of the plain FP32 run stay within bands of the FP64 GPU run (the flow is chaotic: single
+    particles decorrelate after ~30 steps)."""
+    pos = c0_scene(sphlib)
+    ctx = {p: sphlib.SphContext(C0_BOX, pos.shape[0], precision=p, gravity=G981) for p in (0, 1)}
+    for c in ctx.values():
+        c.upload(pos)
+    worst = {"mean": 0.0, "max": 0.0, "ke": 0.0}
+    for step in range(200):
+        for c in ctx.values():
+            c.step(1)
+        if step % 10 == 9:
+            s32, s64 = ctx[0].stats(), ctx[1].stats()
+            assert s32["count"] == s64["count"] == pos.shape[0]
+            assert s32["mass"] == s64["mass"]
+            worst["mean"] = max(worst["mean"], abs(s32["rho_mean"] - s64["rho_mean"]) / s64["rho_mean"])
+            worst["max"] = max(worst["max"], abs(s32["rho_max"] - s64["rho_max"]) / s64["rho_max"])
+            if s64["kinetic"] > 1e-3:
+                worst["ke"] = max(worst["ke"], abs(s32["kinetic"] - s64["kinetic"]) / s64["kinetic"])
+    assert worst["mean"] < 2e-2 and worst["max"] < 2e-1 and worst["ke"] < 3e-1, worst
+    d = ctx[0].download()
+    assert np.all(np.isfinite(d["pos"])) and np.all(np.isfinite(d["rho"]))
+
+
+# ------------------------------------------------------------------------- batches
+def test_batch_equals_single_scenes(sphlib):
+    """Scenes stepped together in one launch per pass give bit-identical results to each
+    scene alone."""
+    dims, boxes = sphlib.batch_plan(5, seed=9, nmin=500, nmax=6000)
+    parts = [sphlib.dam_break_scene(tuple(int(x) for x in d), tuple(float(x) for x in b), seed=s)
+             for s, (d, b) in enumerate(zip(dims, boxes))]
+    counts = [p.shape[0] for p in parts]
+    batch = sphlib.SphContext(boxes, counts, gravity=G981, flags=2)
+    batch.upload(np.concatenate(parts), None, counts)
+    batch.step(10)
+    got = batch.download(acc=True)
+    off = np.concatenate([[0], np.cumsum(counts)])
+    for s, p in enumerate(parts):
+        one = gpu_run(sphlib, boxes[s], p, steps=10, gravity=G981)
+        for k in ("pos", "vel", "rho", "p", "acc"):
+            assert np.array_equal(got[k][off[s]:off[s + 1]], one[k]), (s, k)
+    batch.close()
+
+
+def test_determinism(sphlib):
+    pos = c0_scene(sphlib)
+    a = gpu_run(sphlib, C0_BOX, pos, steps=25, gravity=G981)
+    b = gpu_run(sphlib, C0_BOX, pos, steps=25, gravity=G981)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_graph_replay_matches_passes(sphlib):
+    """sph_step (graph-captured steps) equals the pass-by-pass calls bit for bit."""
+    pos = c0_scene(sphlib, dims=(10, 10, 10))
+    a = gpu_run(sphlib, C0_BOX, pos, steps=19, gravity=G981)
+    ctx = sphlib.SphContext(C0_BOX, pos.shape[0], gravity=G981, flags=2)
+    ctx.upload(pos)
+    for _ in range(19):
+        ctx.pass_grid()
+        ctx.pass_density()
+        ctx.pass_forces()
+    b = ctx.download(acc=True)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+# ------------------------------------------------------------------------- emitters, interface
+def test_append_between_steps(sphlib, oracle_mod):
+    box = (0.6, 0.6, 0.6)
+    ctx = sphlib.SphContext(box, 5000)
+    ctx.upload(np.zeros((0, 3), np.float32))
+    added = []
+    for k in range(6):
+        xyz, vel = sphlib.fountain_emit(seed=4, step=k, n=100, center=(0.0, -0.29, 0.0), radius=0.05, speed=1.0,
+                                        sigma=0.05)
+        ctx.append(0, xyz, vel)
+        added.append(xyz)
+        ctx.step(1)
+    assert ctx.n == 600 and list(ctx.counts()) == [600]
+    d = ctx.download()
+    assert np.all(np.isfinite(d["pos"]))
+    # the first batch moved upward; ids stayed attached to their particles
+    assert np.all(d["pos"][:100, 1] > added[0][:, 1])
+    with pytest.raises(sphlib.SphError) as e:
+        ctx.append(0, np.zeros((4401, 3), np.float32))
+    assert e.value.code == sphlib.SPH_ERR_CAPACITY
+    ctx.close()
+
+
+def test_reference_shaped_simulator(sphlib, oracle_mod):
+    """The CBaseParticleSimulator mirror: setupScene + step on the 0.4 m dam break matches the
+    oracle, and the FOUNTAIN scenario emits 7 particles per step."""
+    sim = sphlib.CCUDAParticleSimulator(0.4, sphlib.DAM_BREAK)
+    sim.setupScene()
+    assert sim.getParticlesCount() == 1620 and "sm_" in sim.getSelectedDevice()
+    sim.step()
+    t = sim.lastPassTimes()
+    assert t[0] > 0 and t[1] > 0 and t[2] > 0 and t[3] == 0 and t[4] == 0
+    got = sim.ctx.download()
+    ref = oracle_run(oracle_mod, 0.4, oracle_mod.reference_dam_break(0.4))
+    errs = rel_errors({k: got[k] for k in ("rho", "p", "pos", "vel")}, ref)
+    assert_within(errs, "mirror")
+    f = sphlib.CCUDAParticleSimulator(0.4, sphlib.FOUNTAIN)
+    f.setupScene()
+    for _ in range(5):
+        f.step()
+    assert f.getParticlesCount() == 35 and f.ctx.n == 35
+    assert f.getMaxParticlesCount() == 1620
+
+
+def test_errors_are_status_codes(sphlib):
+    ctx = sphlib.SphContext((0.4, 0.4, 0.4), 10)
+    with pytest.raises(sphlib.SphError) as e:
+        ctx.step(1)
+    assert e.value.code == sphlib.SPH_ERR_STATE
+    with pytest.raises(sphlib.SphError) as e:
+        ctx.upload(np.zeros((11, 3), np.float32))
+    assert e.value.code == sphlib.SPH_ERR_CAPACITY
+    ctx.upload(np.zeros((3, 3), np.float32) + np.float32([[0.0, 0, 0], [0.01, 0, 0], [0.0, 0.01, 0]]))
+    with pytest.raises(sphlib.SphError) as e:
+        ctx.pass_density()
+    assert e.value.code == sphlib.SPH_ERR_STATE
+    msgs = []
+    sim = sphlib.CCUDAParticleSimulator(0.4, sphlib.DAM_BREAK)
+    sim.errorOccured = msgs.append
+    sim.setupScene()
+    sim.ctx.pass_grid()  # leaves a pass in progress: the next step fails and stops the simulator
+    sim.start()
+    sim.step()
+    assert msgs and not sim.running
+    ctx.close()
+
+
+def test_stats_fp64(sphlib):
+    pos = c0_scene(sphlib, dims=(10, 10, 10))
+    rng = np.random.default_rng(3)
+    vel = rng.normal(0, 0.3, pos.shape).astype(np.float32)
+    ctx = sphlib.SphContext(C0_BOX, pos.shape[0], gravity=G981)
+    ctx.upload(pos, vel)
+    ctx.step(3)
+    s = ctx.stats()
+    d = ctx.download()
+    m = float(np.float32(0.02))
+    v = d["vel"].astype(np.float64)
+    assert s["count"] == 1000 and s["mass"] == m * 1000
+    np.testing.assert_allclose(s["momentum"], m * v.sum(axis=0), rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(s["kinetic"], 0.5 * m * (v ** 2).sum(), rtol=1e-12)
+    np.testing.assert_allclose(s["rho_mean"], d["rho"].astype(np.float64).mean(), rtol=1e-12)
+    assert s["rho_max"] == float(d["rho"].max())
+    ctx.close()
+
+
+# ------------------------------------------------------------------------- full size
+def test_full_size_1m_properties(sphlib):
+    """The 1,000,000-particle dam break (100^3 lattice, 5 x 5 x 2.5 m): grid bit-exact against
+    the vectorised double hash, canonical order, conservation and finiteness over 20 steps."""
+    box = (5.0, 5.0, 2.5)
+    pos = sphlib.dam_break_scene((100, 100, 100), box, seed=1)
+    ctx = sphlib.SphContext(box, pos.shape[0], gravity=G981)
+    ctx.upload(pos)
+    for rep in range(2):
+        cur = ctx.download()["pos"]
+        ctx.pass_grid()
+        cell, counts, order = ctx.grid()
+        want, res = cells_numpy(cur, box)
+        assert np.array_equal(cell.astype(np.int64), want)
+        assert counts.sum() == 1_000_000 and counts.size == int(np.prod(res))
+        assert np.array_equal(np.bincount(want, minlength=counts.size), counts)
+        cs = cell[order].astype(np.int64)
+        key = cs * (1 << 21) + order
+        assert np.all(np.diff(key) > 0)  # ascending (cell, id): canonical and a permutation
+        ctx.pass_density()
+        ctx.pass_forces()
+        ctx.step(19)
+    s = ctx.stats()
+    assert s["count"] == 1_000_000
+    d = ctx.download()
+    assert np.all(np.isfinite(d["pos"])) and np.all(np.isfinite(d["vel"]))
+    assert 900 < s["rho_mean"] < 1200
+    ctx.close()
