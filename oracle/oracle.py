@@ -22,11 +22,18 @@ REF, CANON, F64 = 0, 1, 2
 _lib = None
 
 
+CFLAGS = ["-std=gnu11", "-O2", "-fPIC", "-shared", "-fopenmp", "-Wall", "-Wextra", "-Wno-unused-parameter",
+          # no fused multiply-add: the reference's x86-64 build has none
+          "-ffp-contract=off"]
+
+
 def build(force=False):
-    """Compile liboracle.so with the Makefile beside this file."""
+    """Compile liboracle.so from sph_oracle.c with gcc (one translation unit)."""
     src = os.path.join(HERE, "sph_oracle.c")
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
-        subprocess.check_call(["make", "-s", "-C", HERE])
+        tmp = LIB_PATH + ".tmp"
+        subprocess.check_call([os.environ.get("CC", "gcc"), *CFLAGS, "-o", tmp, src, "-lm"])
+        os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
 
@@ -41,6 +48,7 @@ def lib():
         L.orc_destroy.argtypes = [vp]
         L.orc_set_gravity.argtypes = [vp, ctypes.c_float, ctypes.c_float, ctypes.c_float]
         L.orc_set_dt.argtypes = [vp, ctypes.c_float]
+        L.orc_set_obstacles.argtypes = [vp, ctypes.c_int, fp]
         L.orc_count.argtypes = [vp]
         L.orc_count.restype = ctypes.c_int
         L.orc_get_res.argtypes = [vp, ip]
@@ -101,7 +109,7 @@ def cell_axis(p, box, res):
 class Oracle:
     """One scene of the restated CPU simulator. Particles are kept in id order."""
 
-    def __init__(self, box, mode=REF, threads=None, gravity=None, dt=None):
+    def __init__(self, box, mode=REF, threads=None, gravity=None, dt=None, obstacles=None):
         L = lib()
         if np.isscalar(box):
             box = (box, box, box)
@@ -114,6 +122,9 @@ class Oracle:
             L.orc_set_gravity(self.h, *[ctypes.c_float(g) for g in gravity])
         if dt is not None:
             L.orc_set_dt(self.h, ctypes.c_float(dt))
+        if obstacles is not None and len(obstacles):
+            ob = np.ascontiguousarray(obstacles, np.float32).reshape(-1, 6)
+            L.orc_set_obstacles(self.h, ob.shape[0], _f(ob))
 
     def close(self):
         if self.h:

@@ -110,6 +110,8 @@ typedef struct orc_sim {
     v3d *pos64, *vel64, *acc64;
     double *rho64, *prs64;
     float *ascale;   /* per-particle magnitude of the force terms, for tolerances */
+    int nobs;        /* axis-aligned box obstacles: lo xyz, hi xyz */
+    float *obs;
     int32_t *cell;   /* cell of each particle after the last grid update */
     ilist *cells;
 } orc_sim;
@@ -187,7 +189,7 @@ void orc_destroy(orc_sim *s)
     free(s->cells);
     free(s->pos); free(s->vel); free(s->acc); free(s->rho); free(s->prs);
     free(s->pos64); free(s->vel64); free(s->acc64); free(s->rho64); free(s->prs64);
-    free(s->ascale); free(s->cell);
+    free(s->ascale); free(s->cell); free(s->obs);
     free(s);
 }
 
@@ -196,6 +198,21 @@ void orc_set_gravity(orc_sim *s, float gx, float gy, float gz)
     s->gravity[0] = gx; s->gravity[1] = gy; s->gravity[2] = gz;
 }
 void orc_set_dt(orc_sim *s, float dt) { s->dt = dt; }
+
+/* Box obstacles (no reference counterpart: CCollisionGeometry only bounds the domain).
+ * A particle inside an obstacle grown by the particle radius is pushed out through the
+ * nearest face with the wall spring and damping constants; obstacles act after the walls,
+ * in table order. boxes: 6 floats per obstacle (lo xyz, hi xyz). */
+void orc_set_obstacles(orc_sim *s, int n, const float *boxes)
+{
+    free(s->obs);
+    s->obs = NULL;
+    s->nobs = n > 0 ? n : 0;
+    if (s->nobs) {
+        s->obs = (float *) malloc((size_t) n * 6 * sizeof(float));
+        memcpy(s->obs, boxes, (size_t) n * 6 * sizeof(float));
+    }
+}
 int orc_count(orc_sim *s) { return s->n; }
 void orc_get_res(orc_sim *s, int *res3) { res3[0] = s->res[0]; res3[1] = s->res[1]; res3[2] = s->res[2]; }
 
@@ -385,6 +402,27 @@ static v3f wall_bounce(const orc_sim *s, v3f pos, v3f vel, float *mag)
             m += v3_norm(t1) + v3_norm(t2);
         }
     }
+    for (int o = 0; o < s->nobs; o++) {
+        const float *lo = s->obs + 6 * o, *hi = lo + 3;
+        const float p3[3] = {pos.x, pos.y, pos.z}, vv[3] = {vel.x, vel.y, vel.z};
+        float best = 1e30f;
+        int bf = -1, outside = 0;
+        for (int f = 0; f < 6; f++) {
+            const int a = f % 3;
+            const float dpen = f < 3 ? (p3[a] - lo[a]) + (float) WALL_RADIUS : (hi[a] - p3[a]) + (float) WALL_RADIUS;
+            if (dpen <= 0.0f) outside = 1;
+            else if (dpen < best) { best = dpen; bf = f; }
+        }
+        if (!outside && bf >= 0) {
+            const int a = bf % 3;
+            const float sgn = bf < 3 ? -1.0f : 1.0f;
+            const float kt = (sgn * (float) WALL_K) * best;
+            const float dt = sgn * ((float) WALL_DAMPING * (vv[a] * sgn));
+            float *c = a == 0 ? &acc.x : (a == 1 ? &acc.y : &acc.z);
+            *c = (*c + kt) + dt;
+            m += fabsf(kt) + fabsf(dt);
+        }
+    }
     if (mag) *mag = m;
     return acc;
 }
@@ -404,6 +442,27 @@ static v3d wall_bounce64(const orc_sim *s, v3d pos, v3d vel, double *mag)
             v3d t2 = d3_mul(inv, WALL_DAMPING * d3_dot(vel, inv));
             acc = d3_add(d3_add(acc, t1), t2);
             m += d3_norm(t1) + d3_norm(t2);
+        }
+    }
+    for (int o = 0; o < s->nobs; o++) {
+        const float *lo = s->obs + 6 * o, *hi = lo + 3;
+        const double p3[3] = {pos.x, pos.y, pos.z}, vv[3] = {vel.x, vel.y, vel.z};
+        double best = 1e300;
+        int bf = -1, outside = 0;
+        for (int f = 0; f < 6; f++) {
+            const int a = f % 3;
+            const double dpen = f < 3 ? (p3[a] - lo[a]) + WALL_RADIUS : (hi[a] - p3[a]) + WALL_RADIUS;
+            if (dpen <= 0.0) outside = 1;
+            else if (dpen < best) { best = dpen; bf = f; }
+        }
+        if (!outside && bf >= 0) {
+            const int a = bf % 3;
+            const double sgn = bf < 3 ? -1.0 : 1.0;
+            const double kt = (sgn * WALL_K) * best;
+            const double dt = sgn * (WALL_DAMPING * (vv[a] * sgn));
+            double *c = a == 0 ? &acc.x : (a == 1 ? &acc.y : &acc.z);
+            *c = (*c + kt) + dt;
+            m += fabs(kt) + fabs(dt);
         }
     }
     if (mag) *mag = m;

@@ -341,8 +341,18 @@ def test_full_size_1m_properties(sphlib):
         ctx.pass_forces()
         ctx.step(19)
     s = ctx.stats()
-    assert s["count"] == 1_000_000
+    assert s["count"] == 1_000_000 and s["mass"] == float(np.float32(0.02)) * 1_000_000
     d = ctx.download()
     assert np.all(np.isfinite(d["pos"])) and np.all(np.isfinite(d["vel"]))
-    assert 900 < s["rho_mean"] < 1200
+    # with the reference's soft equation of state (k = 3) the 2.3 m column compresses under
+    # gravity: densities rise well above rest density; the FP64 run of the same 40 steps
+    # must agree on the aggregates
+    ctx64 = sphlib.SphContext(box, pos.shape[0], gravity=G981, precision=sphlib.SPH_F64)
+    ctx64.upload(pos)
+    ctx64.step(40)
+    s64 = ctx64.stats()
+    assert abs(s["rho_mean"] - s64["rho_mean"]) / s64["rho_mean"] < 1e-3
+    assert abs(s["kinetic"] - s64["kinetic"]) / s64["kinetic"] < 1e-2
+    np.testing.assert_allclose(s["rho_mean"], d["rho"].astype(np.float64).mean(), rtol=1e-9)
+    ctx64.close()
     ctx.close()
