@@ -10,9 +10,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <new>
+#include <sstream>
 #include <string>
+#include <sys/stat.h>
 #include <vector>
 
 #include "../../include/sph_cuda.h"
@@ -57,6 +61,8 @@ struct sph_ctx {
     int graph_steps = 0;
     uint32_t graph_n = 0;
     std::vector<uint32_t> scene_off_host;
+    Tune tune;
+    bool tune_pinned = false;  // variants set explicitly: the cache does not override them
 };
 
 namespace {
@@ -180,6 +186,7 @@ int allocate(sph_ctx *c)
         {(void **) &b.st_rho64, rs == 8 ? 8 * N : 0}, {(void **) &b.st_p64, rs == 8 ? 8 * N : 0},
         {(void **) &b.st_acc64, rs == 8 && rec ? 24 * N : 0},
         {(void **) &b.stats, 64 * c->sc.size()},
+        {(void **) &b.stats_partial, 6 * 8 * 64 * c->sc.size()},
     };
     size_t total = 0;
     for (auto &it : items) total += (it.bytes + 255) & ~size_t(255);
@@ -291,14 +298,14 @@ int run_grid(sph_ctx *c)
 template <class R>
 int run_density(sph_ctx *c)
 {
-    CK(c, Launch<R>::density(c->b, c->n, make_consts<R>(c->prm), c->stream));
+    CK(c, Launch<R>::density(c->b, c->n, make_consts<R>(c->prm), c->tune, c->stream));
     return SPH_OK;
 }
 template <class R>
 int run_forces(sph_ctx *c)
 {
     CK(c, Launch<R>::forces(c->b, c->n, make_consts<R>(c->prm), (c->prm.flags & SPH_FLAG_RECORD_ACC) != 0,
-                            c->stream));
+                            c->tune, c->stream));
     return SPH_OK;
 }
 
@@ -364,6 +371,63 @@ int build_graph(sph_ctx *c, int steps)
     c->graph_steps = steps;
     c->graph_n = c->n;
     return SPH_OK;
+}
+
+bool valid_density(int v) { return v == 0 || v == 1 || v == 2 || v == 4; }
+bool valid_forces(int v) { return v >= 0 && v <= 2; }
+
+int bucket_of(uint64_t n)
+{
+    int b = 0;
+    while (n > 1) {
+        n >>= 1;
+        b++;
+    }
+    return b;
+}
+
+std::string tune_cache_path()
+{
+    const char *env = std::getenv("SPH_TUNE_CACHE");
+    if (env && *env) return env;
+    const char *home = std::getenv("HOME");
+    return std::string(home && *home ? home : "/tmp") + "/.cache/sph_gb300/tune.txt";
+}
+
+std::string tune_key(const sph_ctx *c, uint64_t n)
+{
+    std::string dev = c->devname;
+    for (auto &ch : dev)
+        if (ch == ' ' || ch == '|') ch = '_';
+    return dev + "|p" + std::to_string(c->prm.precision) + "|b" + std::to_string(bucket_of(n));
+}
+
+// cached (density, forces) variants for key, if any
+bool tune_lookup(const std::string &key, int &dv, int &fv)
+{
+    std::ifstream f(tune_cache_path());
+    std::string line;
+    bool found = false;
+    while (std::getline(f, line)) {
+        std::istringstream is(line);
+        std::string k;
+        int d, fo;
+        if (is >> k >> d >> fo && k == key && valid_density(d) && valid_forces(fo)) {
+            dv = d;
+            fv = fo;
+            found = true;  // the last entry wins
+        }
+    }
+    return found;
+}
+
+void tune_store(const std::string &key, int dv, int fv)
+{
+    const std::string path = tune_cache_path();
+    for (size_t p = path.find('/', 1); p != std::string::npos; p = path.find('/', p + 1))
+        mkdir(path.substr(0, p).c_str(), 0755);
+    std::ofstream f(path, std::ios::app);
+    if (f) f << key << " " << dv << " " << fv << "\n";
 }
 
 float elapsed(cudaEvent_t a, cudaEvent_t b)
@@ -470,6 +534,11 @@ int sph_upload(sph_ctx *c, const float *xyz, const float *vel, const uint32_t *c
             else
                 CK(c, Launch<float>::ingest(c->b, c->b.st_xyz, vel ? c->b.st_vel : nullptr, 0, c->n, -1, 0,
                                             (uint32_t) c->sc.size(), make_consts<float>(c->prm), c->stream));
+        }
+        int dv, fv;
+        if (!c->tune_pinned && tune_lookup(tune_key(c, total), dv, fv)) {
+            c->tune.density_p = dv;
+            c->tune.forces_mode = fv;
         }
         c->state = HASHED;
         c->n_sorted = 0;
@@ -607,6 +676,88 @@ int sph_step(sph_ctx *c, int32_t nsteps)
         if (rc) return rc;
     }
     CK(c, cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_set_variant(sph_ctx *c, int32_t density_variant, int32_t forces_variant)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (!valid_density(density_variant) || !valid_forces(forces_variant))
+        return fail(c, SPH_ERR_ARG, "unknown launch variant");
+    c->tune.density_p = density_variant;
+    c->tune.forces_mode = forces_variant;
+    c->tune_pinned = true;
+    drop_graph(c);
+    return SPH_OK;
+}
+
+int sph_get_variant(const sph_ctx *c, int32_t out[2])
+{
+    if (!c || !out) return SPH_ERR_ARG;
+    out[0] = c->tune.density_p;
+    out[1] = c->tune.forces_mode;
+    return SPH_OK;
+}
+
+int sph_autotune(sph_ctx *c, int32_t reps)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (reps < 1) return fail(c, SPH_ERR_ARG, "reps must be >= 1");
+    if (c->state != HASHED) return fail(c, SPH_ERR_STATE, "autotune needs a completed step (or an upload)");
+    if (c->n == 0) return fail(c, SPH_ERR_STATE, "autotune needs particles");
+    CK(c, cudaSetDevice(c->device));
+    drop_graph(c);
+    int rc = pass_grid(c);
+    if (rc) return rc;
+    const int dvs[4] = {0, 1, 2, 4};
+    float best = 1e30f;
+    int bd = c->tune.density_p;
+    for (int dv : dvs) {
+        c->tune.density_p = dv;
+        for (int r = 0; r <= reps; r++) {  // the first run is a warm-up
+            CK(c, cudaEventRecord(c->ev[0], c->stream));
+            c->state = SORTED;
+            rc = pass_density(c);
+            if (rc) return rc;
+            CK(c, cudaEventRecord(c->ev[1], c->stream));
+            CK(c, cudaEventSynchronize(c->ev[1]));
+            const float ms = elapsed(c->ev[0], c->ev[1]);
+            if (r > 0 && ms < best) {
+                best = ms;
+                bd = dv;
+            }
+        }
+    }
+    c->tune.density_p = bd;
+    c->state = SORTED;
+    rc = pass_density(c);
+    if (rc) return rc;
+    best = 1e30f;
+    int bf = c->tune.forces_mode;
+    for (int fv = 0; fv <= 2; fv++) {
+        c->tune.forces_mode = fv;
+        for (int r = 0; r <= reps; r++) {
+            CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));  // the pass adds to the counts
+            CK(c, cudaEventRecord(c->ev[2], c->stream));
+            c->state = DENSE;
+            rc = pass_forces(c);
+            if (rc) return rc;
+            CK(c, cudaEventRecord(c->ev[3], c->stream));
+            CK(c, cudaEventSynchronize(c->ev[3]));
+            const float ms = elapsed(c->ev[2], c->ev[3]);
+            if (r > 0 && ms < best) {
+                best = ms;
+                bf = fv;
+            }
+        }
+    }
+    c->tune.forces_mode = bf;
+    CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
+    c->state = DENSE;
+    rc = pass_forces(c);
+    if (rc) return rc;
+    c->tune_pinned = true;
+    tune_store(tune_key(c, c->n), bd, bf);
     return SPH_OK;
 }
 

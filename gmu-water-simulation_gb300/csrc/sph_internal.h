@@ -60,6 +60,7 @@ struct DevBufs {
     float *st_xyz, *st_vel, *st_rho, *st_p, *st_acc;
     double *st_xyz64, *st_vel64, *st_rho64, *st_p64, *st_acc64;
     double *stats;         // per-scene FP64 reductions, 8 doubles each
+    double *stats_partial; // per-scene slices of the reductions (kSplit x 6 doubles each)
 };
 
 // ---- exact cell hash -------------------------------------------------------------
@@ -92,6 +93,16 @@ __host__ __device__ inline int cell_axis(double p, float half, float inv_h, doub
     return (int) floor(q);
 }
 
+// Launch variants of the neighbour kernels (picked per context; see the autotuner).
+//   density_p : 0 = one particle per thread, first form; 1/2/4 = blocked branchless form
+//               with that many consecutive particles per thread
+//   forces_mode: 0 = pair terms inside the candidate loop; 1/2 = compacted neighbour list
+//               of 32/64 entries per thread in shared memory
+struct Tune {
+    int density_p = 2;
+    int forces_mode = 2;
+};
+
 // ---- kernel launchers (sph_kernels.cu) --------------------------------------------
 template <class R>
 struct Launch {
@@ -102,8 +113,9 @@ struct Launch {
                               int32_t scene, uint32_t id0, uint32_t nscenes, Consts<R> c, cudaStream_t st);
     static cudaError_t scan(const DevBufs &b, uint32_t ncells, cudaStream_t st);
     static cudaError_t permute(const DevBufs &b, uint32_t n, cudaStream_t st);
-    static cudaError_t density(const DevBufs &b, uint32_t n, Consts<R> c, cudaStream_t st);
-    static cudaError_t forces(const DevBufs &b, uint32_t n, Consts<R> c, bool record_acc, cudaStream_t st);
+    static cudaError_t density(const DevBufs &b, uint32_t n, Consts<R> c, const Tune &t, cudaStream_t st);
+    static cudaError_t forces(const DevBufs &b, uint32_t n, Consts<R> c, bool record_acc, const Tune &t,
+                              cudaStream_t st);
     // state of the first n_state particles, density/pressure of the first n_aux, and
     // accelerations of the first n_acc (when recorded) into id-ordered staging arrays
     static cudaError_t egress(const DevBufs &b, uint32_t n_state, uint32_t n_aux, uint32_t n_acc, int layout_sorted,

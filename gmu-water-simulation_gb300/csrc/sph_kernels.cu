@@ -297,6 +297,19 @@ __global__ void __launch_bounds__(256) k_rank_permute(const uint2 *__restrict__ 
     st4(vel_s + dst, ld4(vel_u + i));
 }
 
+// (h^2 - r^2)^3 for r^2 <= h^2, else 0, branchless: t = h^2 - dx^2 - dy^2 - dz^2 clamped at 0.
+// Every density kernel uses this one expression, so all launch variants give the same bits
+// (a candidate outside a particle's own 27 cells is farther than h and adds exactly 0).
+template <class R>
+__device__ __forceinline__ R poly6_term(R dx, R dy, R dz, R h2)
+{
+    R t = h2 - dx * dx;
+    t -= dy * dy;
+    t -= dz * dz;
+    t = t > (R) 0 ? t : (R) 0;
+    return t * t * t;
+}
+
 // ------------------------------------------------------------------------------------
 // Neighbour walk: the 27 cells around a particle are 9 rows (dy, dz) of 3 cells along x,
 // and in (cell, id) order each row is one contiguous range of the sorted arrays.
@@ -343,12 +356,7 @@ __global__ void __launch_bounds__(256) k_density(const Vec4<R> *__restrict__ pos
 #pragma unroll 4
         for (uint32_t j = jb; j < je; j++) {
             const Vec4<R> pj = ld4(pos + j);
-            const R dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            const R r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 <= h2) {
-                const R t = h2 - r2;
-                acc += t * t * t;
-            }
+            acc += poly6_term<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
         }
     });
     const R rho = rmul(rmul(acc, c.c_poly6), c.mass);
@@ -356,99 +364,66 @@ __global__ void __launch_bounds__(256) k_density(const Vec4<R> *__restrict__ pos
     st4(aux + i, Vec4<R>{rho, p, rdiv(p, rmul(rho, rho)), rdiv((R) 1, rho)});
 }
 
-// Forces (src/CCPUParticleSimulator.cpp:143-203), walls (src/CCollisionGeometry.cpp:117-133),
-// obstacles, position-Verlet integration (src/CCPUParticleSimulator.cpp:211-229) and the
-// cell hash of the new position for the next step, in one pass.
+// The two walls of one axis (src/CCollisionGeometry.cpp:117-133 restated per component).
 template <class R>
-__global__ void __launch_bounds__(256) k_forces(const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel,
-                                                const Vec4<R> *__restrict__ aux, const uint32_t *__restrict__ start,
-                                                const SceneDev *__restrict__ scenes,
-                                                const ObstacleDev *__restrict__ obstacles, uint32_t n, Consts<R> c,
+__device__ __forceinline__ void wall_axis(R p, R v, R half, const Consts<R> &c, R &acc)
+{
+    R d = radd(rmul(rsub(-half, p), (R) 1), c.wall_r);  // min wall, inverse normal +1
+    if (d > (R) 0) acc = radd(radd(acc, rmul(rmul((R) 1, c.wall_k), d)), rmul((R) 1, rmul(c.wall_damp, rmul(v, (R) 1))));
+    d = radd(rmul(rsub(half, p), (R) -1), c.wall_r);    // max wall, inverse normal -1
+    if (d > (R) 0)
+        acc = radd(radd(acc, rmul(rmul((R) -1, c.wall_k), d)), rmul((R) -1, rmul(c.wall_damp, rmul(v, (R) -1))));
+}
+
+// Per-particle epilogue of the force pass: total acceleration from the summed pressure and
+// viscosity terms (src/CCPUParticleSimulator.cpp:189-193), walls (src/CCollisionGeometry.cpp:117-133),
+// box obstacles, position-Verlet integration (src/CCPUParticleSimulator.cpp:211-229), and the
+// cell hash of the new position for the next step. Float operations are explicitly rounded
+// in the reference's order.
+template <class R>
+__device__ __forceinline__ void finish_particle(uint32_t i, const Vec4<R> &pi, const Vec4<R> &vi, R rho,
+                                                const SceneDev &sc, const ObstacleDev *__restrict__ obstacles,
+                                                const Consts<R> &c, R fpx, R fpy, R fpz, R fvx, R fvy, R fvz,
                                                 Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out,
                                                 Vec4<R> *__restrict__ acc_out, uint2 *__restrict__ cid_out,
                                                 uint32_t *__restrict__ count)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const Vec4<R> pi = ld4(pos + i);
-    const Vec4<R> vi = ld4(vel + i);
-    const Vec4<R> ai = ld4(aux + i);
-    const uint32_t s = wbits(pi.w), id = wbits(vi.w);
-    const SceneDev sc = load_scene(scenes, s);
-    int cx, cy, cz;
-    hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
-    const R h = c.h, h2 = c.h2, qi = ai.z;
-    R fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
-    for_each_row<R>(sc, start, cx, cy, cz, [&](uint32_t jb, uint32_t je) {
-#pragma unroll 2
-        for (uint32_t j = jb; j < je; j++) {
-            const Vec4<R> pj = ld4(pos + j);
-            const R dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            const R r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 <= h2 && j != i) {
-                const Vec4<R> vj = ld4(vel + j);
-                R qj, invj;
-                ld_qinv(aux + j, qj, invj);
-                const R rinv = inv_sqrt(r2);
-                const R hr = h - r2 * rinv;
-                const R w = (qi + qj) * (c.c_spiky * hr * hr * rinv);  // (p_i/rho_i^2 + p_j/rho_j^2) grad W
-                fpx += w * dx;
-                fpy += w * dy;
-                fpz += w * dz;
-                const R l = c.c_visc * hr * invj;                      // lap W / rho_j
-                fvx += (vj.x - vi.x) * l;
-                fvy += (vj.y - vi.y) * l;
-                fvz += (vj.z - vi.z) * l;
-            }
-        }
-    });
-    const R rho = ai.x;
     const R sp = rmul(-c.mass, rho), sv = rmul(c.mu, c.mass);
     R ax = rdiv(radd(radd(rmul(fpx, sp), rmul(fvx, sv)), rmul((R) sc.gravity[0], rho)), rho);
     R ay = rdiv(radd(radd(rmul(fpy, sp), rmul(fvy, sv)), rmul((R) sc.gravity[1], rho)), rho);
     R az = rdiv(radd(radd(rmul(fpz, sp), rmul(fvz, sv)), rmul((R) sc.gravity[2], rho)), rho);
 
-    // walls at -+box/2 in the order left, bottom, back, right, top, front; the inverse
-    // normal of wall w points into the box along axis w % 3
+    // walls at -+box/2 in the order left, bottom, back, right, top, front. Each wall acts on
+    // one component only, so per axis: the min wall (inverse normal +1), then the max wall
+    // (inverse normal -1); d = dot(wall - p, n_inv) + r, a += K n_inv d + damp dot(v, n_inv) n_inv.
     R wx = 0, wy = 0, wz = 0;
-    const R p3[3] = {pi.x, pi.y, pi.z};
-    const R v3[3] = {vi.x, vi.y, vi.z};
-#pragma unroll
-    for (int w = 0; w < 6; w++) {
-        const int a = w % 3;
-        const R sgn = w < 3 ? (R) 1 : (R) -1;                   // inverse normal component
-        const R wallp = w < 3 ? -(R) sc.half[a] : (R) sc.half[a];
-        const R d = radd(rmul(rsub(wallp, p3[a]), sgn), c.wall_r);
-        if (d > (R) 0) {
-            const R kt = rmul(rmul(sgn, c.wall_k), d);
-            const R dt = rmul(sgn, rmul(c.wall_damp, rmul(v3[a], sgn)));
-            if (a == 0) { wx = radd(radd(wx, kt), dt); }
-            else if (a == 1) { wy = radd(radd(wy, kt), dt); }
-            else { wz = radd(radd(wz, kt), dt); }
-        }
-    }
+    wall_axis<R>(pi.x, vi.x, (R) sc.half[0], c, wx);
+    wall_axis<R>(pi.y, vi.y, (R) sc.half[1], c, wy);
+    wall_axis<R>(pi.z, vi.z, (R) sc.half[2], c, wz);
     // box obstacles: inside the obstacle grown by the particle radius, push out through the
     // nearest face with the wall spring and damping
     for (uint32_t o = 0; o < sc.n_obs; o++) {
         const ObstacleDev ob = obstacles[sc.obs_base + o];
-        R best = (R) 1e30;
-        int bf = -1;
-#pragma unroll
-        for (int f = 0; f < 6; f++) {
-            const int a = f % 3;
-            const R dpen = f < 3 ? radd(rsub(p3[a], (R) ob.lo[a]), c.wall_r) : radd(rsub((R) ob.hi[a], p3[a]), c.wall_r);
-            if (dpen <= (R) 0) { bf = -2; }
-            if (bf != -2 && dpen < best) { best = dpen; bf = f; }
-        }
-        if (bf >= 0) {
-            const int a = bf % 3;
-            const R sgn = bf < 3 ? (R) -1 : (R) 1;  // outward normal of the face
-            const R kt = rmul(rmul(sgn, c.wall_k), best);
-            const R dt = rmul(sgn, rmul(c.wall_damp, rmul(v3[a], sgn)));
-            if (a == 0) { wx = radd(radd(wx, kt), dt); }
-            else if (a == 1) { wy = radd(radd(wy, kt), dt); }
-            else { wz = radd(radd(wz, kt), dt); }
-        }
+        const R d0 = radd(rsub(pi.x, (R) ob.lo[0]), c.wall_r), d1 = radd(rsub(pi.y, (R) ob.lo[1]), c.wall_r);
+        const R d2 = radd(rsub(pi.z, (R) ob.lo[2]), c.wall_r), d3 = radd(rsub((R) ob.hi[0], pi.x), c.wall_r);
+        const R d4 = radd(rsub((R) ob.hi[1], pi.y), c.wall_r), d5 = radd(rsub((R) ob.hi[2], pi.z), c.wall_r);
+        if (d0 <= (R) 0 || d1 <= (R) 0 || d2 <= (R) 0 || d3 <= (R) 0 || d4 <= (R) 0 || d5 <= (R) 0) continue;
+        // first face with the smallest penetration, in face order
+        R best = d0;
+        int bf = 0;
+        if (d1 < best) { best = d1; bf = 1; }
+        if (d2 < best) { best = d2; bf = 2; }
+        if (d3 < best) { best = d3; bf = 3; }
+        if (d4 < best) { best = d4; bf = 4; }
+        if (d5 < best) { best = d5; bf = 5; }
+        const R sgn = bf < 3 ? (R) -1 : (R) 1;  // outward normal of the face
+        const R kt = rmul(rmul(sgn, c.wall_k), best);
+        const int a = bf % 3;
+        const R v = a == 0 ? vi.x : (a == 1 ? vi.y : vi.z);
+        const R dt = rmul(sgn, rmul(c.wall_damp, rmul(v, sgn)));
+        if (a == 0) wx = radd(radd(wx, kt), dt);
+        else if (a == 1) wy = radd(radd(wy, kt), dt);
+        else wz = radd(radd(wz, kt), dt);
     }
     ax = radd(ax, wx);
     ay = radd(ay, wy);
@@ -466,7 +441,208 @@ __global__ void __launch_bounds__(256) k_forces(const Vec4<R> *__restrict__ pos,
     int qx, qy, qz;
     const uint32_t cell = hash_cell<R>(sc, nx, ny, nz, c, qx, qy, qz);
     atomicAdd(count + cell, 1u);
-    cid_out[i] = make_uint2(cell, id);
+    cid_out[i] = make_uint2(cell, wbits(vi.w));
+}
+
+// Pressure and viscosity terms of one accepted neighbour (src/CCPUParticleSimulator.cpp:177-183).
+template <class R>
+__device__ __forceinline__ void pair_force(const Vec4<R> &pi, const Vec4<R> &vi, R qi, uint32_t j,
+                                           const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel,
+                                           const Vec4<R> *__restrict__ aux, const Consts<R> &c, R &fpx, R &fpy,
+                                           R &fpz, R &fvx, R &fvy, R &fvz)
+{
+    const Vec4<R> pj = ld4(pos + j);
+    const Vec4<R> vj = ld4(vel + j);
+    R qj, invj;
+    ld_qinv(aux + j, qj, invj);
+    const R dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    const R r2 = dx * dx + dy * dy + dz * dz;
+    const R rinv = inv_sqrt(r2);
+    const R hr = c.h - r2 * rinv;
+    const R w = (qi + qj) * (c.c_spiky * hr * hr * rinv);  // (p_i/rho_i^2 + p_j/rho_j^2) grad W
+    fpx += w * dx;
+    fpy += w * dy;
+    fpz += w * dz;
+    const R l = c.c_visc * hr * invj;                      // lap W / rho_j
+    fvx += (vj.x - vi.x) * l;
+    fvy += (vj.y - vi.y) * l;
+    fvz += (vj.z - vi.z) * l;
+}
+
+// Forces, first form: one thread per sorted particle, the pair terms evaluated inside the
+// candidate loop.
+template <class R>
+__global__ void __launch_bounds__(256) k_forces(const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel,
+                                                const Vec4<R> *__restrict__ aux, const uint32_t *__restrict__ start,
+                                                const SceneDev *__restrict__ scenes,
+                                                const ObstacleDev *__restrict__ obstacles, uint32_t n, Consts<R> c,
+                                                Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out,
+                                                Vec4<R> *__restrict__ acc_out, uint2 *__restrict__ cid_out,
+                                                uint32_t *__restrict__ count)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Vec4<R> pi = ld4(pos + i);
+    const Vec4<R> vi = ld4(vel + i);
+    const Vec4<R> ai = ld4(aux + i);
+    const SceneDev sc = load_scene(scenes, wbits(pi.w));
+    int cx, cy, cz;
+    hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
+    const R h2 = c.h2, qi = ai.z;
+    R fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
+    for_each_row<R>(sc, start, cx, cy, cz, [&](uint32_t jb, uint32_t je) {
+#pragma unroll 2
+        for (uint32_t j = jb; j < je; j++) {
+            const Vec4<R> pj = ld4(pos + j);
+            const R dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            const R r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 <= h2 && j != i) pair_force<R>(pi, vi, qi, j, pos, vel, aux, c, fpx, fpy, fpz, fvx, fvy, fvz);
+        }
+    });
+    finish_particle<R>(i, pi, vi, ai.x, sc, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
+                       cid_out, count);
+}
+
+// Forces, compacted form: the candidate scan only tests distances and appends accepted
+// neighbours to a per-thread list in shared memory (column-major, so a warp's appends hit
+// distinct banks); the pair terms then run over the list with every lane busy. A full
+// list is drained in place, so any neighbour count is handled.
+template <class R, int CAP, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_forces_list(
+    const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
+    const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
+    uint32_t n, Consts<R> c, Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out,
+    Vec4<R> *__restrict__ acc_out, uint2 *__restrict__ cid_out, uint32_t *__restrict__ count)
+{
+    __shared__ uint32_t list[CAP][BLOCK];
+    const uint32_t i = blockIdx.x * BLOCK + threadIdx.x;
+    if (i >= n) return;
+    const Vec4<R> pi = ld4(pos + i);
+    const Vec4<R> vi = ld4(vel + i);
+    const Vec4<R> ai = ld4(aux + i);
+    const SceneDev sc = load_scene(scenes, wbits(pi.w));
+    int cx, cy, cz;
+    hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
+    const R h2 = c.h2, qi = ai.z;
+    R fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
+    int cnt = 0;
+    auto drain = [&]() {
+        for (int k = 0; k < cnt; k++)
+            pair_force<R>(pi, vi, qi, list[k][threadIdx.x], pos, vel, aux, c, fpx, fpy, fpz, fvx, fvy, fvz);
+        cnt = 0;
+    };
+    for_each_row<R>(sc, start, cx, cy, cz, [&](uint32_t jb, uint32_t je) {
+        // chunks of at most CAP candidates; the list is drained between chunks when the
+        // next chunk might not fit, so it never overflows inside the candidate loop
+        for (uint32_t cb = jb; cb < je; cb += CAP) {
+            const uint32_t ce = min(je, cb + (uint32_t) CAP);
+            if (cnt + (int) (ce - cb) > CAP) drain();
+#pragma unroll 4
+            for (uint32_t j = cb; j < ce; j++) {
+                const Vec4<R> pj = ld4(pos + j);
+                const R dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                const R r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 <= h2 && j != i) list[cnt++][threadIdx.x] = j;
+            }
+        }
+    });
+    drain();
+    finish_particle<R>(i, pi, vi, ai.x, sc, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
+                       cid_out, count);
+}
+
+// Density, blocked form: each thread owns P consecutive sorted particles. When they share a
+// scene and a (y, z) row of cells (nearly always in sorted order) one candidate scan over the
+// union x-range serves all of them: a candidate outside a particle's own 3 x 3 x 3 block is
+// farther than h (cells are h wide and the clamp only moves particles outward), so the
+// r^2 test alone selects the same neighbours. The test is branchless: t = h^2 - r^2
+// clamped at 0 contributes t^3.
+template <class R, int P>
+__global__ void __launch_bounds__(256) k_density_blk(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
+                                                     const uint32_t *__restrict__ start,
+                                                     const SceneDev *__restrict__ scenes, uint32_t n, Consts<R> c)
+{
+    const uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) * P;
+    if (i0 >= n) return;
+    R px[P], py[P], pz[P], acc[P];
+    int cxs[P];
+    const Vec4<R> p0 = ld4(pos + i0);
+    const uint32_t s0 = wbits(p0.w);
+    const SceneDev sc = load_scene(scenes, s0);
+    int cy0, cz0;
+    bool same = true;
+#pragma unroll
+    for (int p = 0; p < P; p++) {
+        const uint32_t i = i0 + p;
+        acc[p] = 0;
+        Vec4<R> q = p0;
+        if (p > 0 && i < n) q = ld4(pos + i);
+        px[p] = q.x; py[p] = q.y; pz[p] = q.z;
+        if (p > 0 && i >= n) { px[p] = py[p] = pz[p] = (R) 1e30; cxs[p] = cxs[0]; continue; }
+        int cx, cy, cz;
+        if (p == 0 || wbits(q.w) == s0) {
+            hash_cell<R>(sc, q.x, q.y, q.z, c, cx, cy, cz);
+            if (p == 0) { cy0 = cy; cz0 = cz; }
+            else same = same && cy == cy0 && cz == cz0;
+        } else {
+            same = false;
+            cx = 0;
+        }
+        cxs[p] = cx;
+    }
+    const R h2 = c.h2;
+    if (same) {
+        int lo = cxs[0], hi = cxs[0];
+#pragma unroll
+        for (int p = 1; p < P; p++) { lo = min(lo, cxs[p]); hi = max(hi, cxs[p]); }
+        const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
+        const int xl = lo > 0 ? lo - 1 : 0, xh = hi + 1 < X ? hi + 1 : X - 1;
+#pragma unroll 1
+        for (int dz = -1; dz <= 1; dz++) {
+            const int z = cz0 + dz;
+            if (z < 0 || z >= Z) continue;
+#pragma unroll 1
+            for (int dy = -1; dy <= 1; dy++) {
+                const int y = cy0 + dy;
+                if (y < 0 || y >= Y) continue;
+                const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
+                const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+#pragma unroll 2
+                for (uint32_t j = jb; j < je; j++) {
+                    const Vec4<R> pj = ld4(pos + j);
+#pragma unroll
+                    for (int p = 0; p < P; p++) acc[p] += poly6_term<R>(px[p] - pj.x, py[p] - pj.y, pz[p] - pj.z, h2);
+                }
+            }
+        }
+    } else {
+        // particles of different rows or scenes: one walk each
+#pragma unroll
+        for (int p = 0; p < P; p++) {
+            const uint32_t i = i0 + p;
+            if (i >= n) continue;
+            const Vec4<R> q = ld4(pos + i);
+            const SceneDev sq = load_scene(scenes, wbits(q.w));
+            int cx, cy, cz;
+            hash_cell<R>(sq, q.x, q.y, q.z, c, cx, cy, cz);
+            R a = 0;
+            for_each_row<R>(sq, start, cx, cy, cz, [&](uint32_t jb, uint32_t je) {
+                for (uint32_t j = jb; j < je; j++) {
+                    const Vec4<R> pj = ld4(pos + j);
+                    a += poly6_term<R>(q.x - pj.x, q.y - pj.y, q.z - pj.z, h2);
+                }
+            });
+            acc[p] = a;
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < P; p++) {
+        const uint32_t i = i0 + p;
+        if (i >= n) continue;
+        const R rho = rmul(rmul(acc[p], c.c_poly6), c.mass);
+        const R pr = rmul(c.k, rsub(rho, c.rho0));
+        st4(aux + i, Vec4<R>{rho, pr, rdiv(pr, rmul(rho, rho)), rdiv((R) 1, rho)});
+    }
 }
 
 // ------------------------------------------------------------------------------------
@@ -501,18 +677,27 @@ __global__ void __launch_bounds__(256) k_egress(const Vec4<R> *__restrict__ posL
     }
 }
 
-// FP64 reductions per scene, one block per scene over the scene's contiguous range, fixed
-// reduction order (deterministic): mass, momentum, kinetic energy, mean and max density.
+// FP64 reductions per scene in fixed order (deterministic): STATS_SPLIT blocks per scene
+// each reduce a fixed slice of the scene's contiguous range into a partial record, then one
+// block per scene adds the partials in slice order. Mass, momentum, kinetic energy, mean and
+// max density.
+constexpr int STATS_SPLIT = 64;
+constexpr int STATS_THREADS = 256;
+
 template <class R>
-__global__ void __launch_bounds__(256) k_stats(const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
-                                               const uint32_t *__restrict__ start,
-                                               const SceneDev *__restrict__ scenes, double mass,
-                                               double *__restrict__ out)
+__global__ void __launch_bounds__(STATS_THREADS) k_stats_partial(const Vec4<R> *__restrict__ vel,
+                                                                 const Vec4<R> *__restrict__ aux,
+                                                                 const uint32_t *__restrict__ start,
+                                                                 const SceneDev *__restrict__ scenes,
+                                                                 double *__restrict__ partial)
 {
-    const SceneDev sc = load_scene(scenes, blockIdx.x);
+    const uint32_t s = blockIdx.x / STATS_SPLIT, part = blockIdx.x % STATS_SPLIT;
+    const SceneDev sc = load_scene(scenes, s);
     const uint32_t b = start[sc.cell_base], e = start[sc.cell_base + sc.ncells];
+    const uint32_t len = e - b, chunk = (len + STATS_SPLIT - 1) / STATS_SPLIT;
+    const uint32_t lo = b + part * chunk, hi = min(e, lo + chunk);
     double mx = 0, my = 0, mz = 0, ke = 0, rs = 0, rmax = -1e300;
-    for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += STATS_THREADS) {
         const Vec4<R> v = ldc4(vel + i);
         const Vec4<R> a = ldc4(aux + i);
         const double vx = (double) v.x, vy = (double) v.y, vz = (double) v.z;
@@ -521,11 +706,11 @@ __global__ void __launch_bounds__(256) k_stats(const Vec4<R> *__restrict__ vel, 
         rs += (double) a.x;
         rmax = fmax(rmax, (double) a.x);
     }
-    __shared__ double red[6][256];
+    __shared__ double red[6][STATS_THREADS];
     red[0][threadIdx.x] = mx; red[1][threadIdx.x] = my; red[2][threadIdx.x] = mz;
     red[3][threadIdx.x] = ke; red[4][threadIdx.x] = rs; red[5][threadIdx.x] = rmax;
     __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
+    for (int w = STATS_THREADS / 2; w > 0; w >>= 1) {
         if ((int) threadIdx.x < w) {
 #pragma unroll
             for (int k = 0; k < 5; k++) red[k][threadIdx.x] += red[k][threadIdx.x + w];
@@ -533,16 +718,29 @@ __global__ void __launch_bounds__(256) k_stats(const Vec4<R> *__restrict__ vel, 
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        const double cnt = (double) (e - b);
-        double *o = out + 8 * blockIdx.x;
-        o[0] = mass * cnt;
-        o[1] = mass * red[0][0]; o[2] = mass * red[1][0]; o[3] = mass * red[2][0];
-        o[4] = 0.5 * mass * red[3][0];
-        o[5] = cnt > 0 ? red[4][0] / cnt : 0.0;
-        o[6] = cnt > 0 ? red[5][0] : 0.0;
-        o[7] = cnt;
+    if (threadIdx.x < 6) partial[6 * blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void k_stats_final(const double *__restrict__ partial, const uint32_t *__restrict__ start,
+                              const SceneDev *__restrict__ scenes, double mass, double *__restrict__ out)
+{
+    const uint32_t s = blockIdx.x;
+    if (threadIdx.x != 0) return;
+    const SceneDev sc = load_scene(scenes, s);
+    const double cnt = (double) (start[sc.cell_base + sc.ncells] - start[sc.cell_base]);
+    double t[6] = {0, 0, 0, 0, 0, -1e300};
+    for (int k = 0; k < STATS_SPLIT; k++) {
+        const double *p = partial + 6 * ((size_t) s * STATS_SPLIT + k);
+        for (int q = 0; q < 5; q++) t[q] += p[q];
+        t[5] = fmax(t[5], p[5]);
     }
+    double *o = out + 8 * s;
+    o[0] = mass * cnt;
+    o[1] = mass * t[0]; o[2] = mass * t[1]; o[3] = mass * t[2];
+    o[4] = 0.5 * mass * t[3];
+    o[5] = cnt > 0 ? t[4] / cnt : 0.0;
+    o[6] = cnt > 0 ? t[5] : 0.0;
+    o[7] = cnt;
 }
 
 // ------------------------------------------------------------------------------------
@@ -580,21 +778,41 @@ cudaError_t Launch<R>::permute(const DevBufs &b, uint32_t n, cudaStream_t st)
 }
 
 template <class R>
-cudaError_t Launch<R>::density(const DevBufs &b, uint32_t n, Consts<R> c, cudaStream_t st)
+cudaError_t Launch<R>::density(const DevBufs &b, uint32_t n, Consts<R> c, const Tune &t, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
-    k_density<R><<<nblk(n, 256), 256, 0, st>>>((const Vec4<R> *) b.pos_s, (Vec4<R> *) b.aux, b.start, b.scenes, n, c);
+    const Vec4<R> *pos = (const Vec4<R> *) b.pos_s;
+    Vec4<R> *aux = (Vec4<R> *) b.aux;
+    switch (t.density_p) {
+    case 2: k_density_blk<R, 2><<<nblk((n + 1) / 2, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c); break;
+    case 4: k_density_blk<R, 4><<<nblk((n + 3) / 4, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c); break;
+    case 1: k_density_blk<R, 1><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c); break;
+    default: k_density<R><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c); break;
+    }
     return cudaGetLastError();
 }
 
 template <class R>
-cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool record_acc, cudaStream_t st)
+cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool record_acc, const Tune &t,
+                              cudaStream_t st)
 {
     if (!n) return cudaSuccess;
-    k_forces<R><<<nblk(n, 256), 256, 0, st>>>((const Vec4<R> *) b.pos_s, (const Vec4<R> *) b.vel_s,
-                                              (const Vec4<R> *) b.aux, b.start, b.scenes, b.obstacles, n, c,
-                                              (Vec4<R> *) b.pos_u, (Vec4<R> *) b.vel_u,
-                                              record_acc ? (Vec4<R> *) b.acc : nullptr, b.cid_u, b.count);
+    const Vec4<R> *pos = (const Vec4<R> *) b.pos_s, *vel = (const Vec4<R> *) b.vel_s, *aux = (const Vec4<R> *) b.aux;
+    Vec4<R> *po = (Vec4<R> *) b.pos_u, *vo = (Vec4<R> *) b.vel_u, *ao = record_acc ? (Vec4<R> *) b.acc : nullptr;
+    switch (t.forces_mode) {
+    case 1:
+        k_forces_list<R, 32, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
+                                                                  po, vo, ao, b.cid_u, b.count);
+        break;
+    case 2:
+        k_forces_list<R, 64, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
+                                                                  po, vo, ao, b.cid_u, b.count);
+        break;
+    default:
+        k_forces<R><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c, po, vo, ao,
+                                                  b.cid_u, b.count);
+        break;
+    }
     return cudaGetLastError();
 }
 
@@ -624,7 +842,9 @@ template <class R>
 cudaError_t Launch<R>::stats(const DevBufs &b, uint32_t nscenes, Consts<R> c, int layout_sorted, cudaStream_t st)
 {
     const Vec4<R> *vel = (const Vec4<R> *) (layout_sorted ? b.vel_s : b.vel_u);
-    k_stats<R><<<nscenes, 256, 0, st>>>(vel, (const Vec4<R> *) b.aux, b.start, b.scenes, (double) c.mass, b.stats);
+    k_stats_partial<R><<<nscenes * STATS_SPLIT, STATS_THREADS, 0, st>>>(vel, (const Vec4<R> *) b.aux, b.start, b.scenes,
+                                                                        b.stats_partial);
+    k_stats_final<<<nscenes, 32, 0, st>>>(b.stats_partial, b.start, b.scenes, (double) c.mass, b.stats);
     return cudaGetLastError();
 }
 

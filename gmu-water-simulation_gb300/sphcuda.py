@@ -27,7 +27,7 @@ SPH_FLAG_PROFILE, SPH_FLAG_RECORD_ACC = 1, 2
 # every symbol the header declares
 EXPORTS = (
     "sph_params_default", "sph_create", "sph_batch_create", "sph_destroy", "sph_last_error", "sph_device_name",
-    "sph_stream",
+    "sph_stream", "sph_set_variant", "sph_get_variant", "sph_autotune",
     "sph_upload", "sph_append", "sph_set_gravity", "sph_step", "sph_pass_grid", "sph_pass_density",
     "sph_pass_forces", "sph_pass_times", "sph_get_counts", "sph_num_scenes", "sph_num_particles",
     "sph_get_resolution", "sph_download", "sph_download_f64", "sph_get_grid", "sph_stats",
@@ -84,6 +84,9 @@ def load(path=None):
         "sph_last_error": (ctypes.c_char_p, [vp]),
         "sph_device_name": (ctypes.c_char_p, [vp]),
         "sph_stream": (vp, [vp]),
+        "sph_set_variant": (i32, [vp, i32, i32]),
+        "sph_get_variant": (i32, [vp, ip]),
+        "sph_autotune": (i32, [vp, i32]),
         "sph_upload": (i32, [vp, vp, vp, up]),
         "sph_append": (i32, [vp, u32, vp, vp, u32]),
         "sph_set_gravity": (i32, [vp, i32, fp]),
@@ -299,6 +302,18 @@ class SphContext:
 
     def pass_forces(self):
         self._ck(load().sph_pass_forces(self.h))
+
+    def set_variant(self, density, forces):
+        self._ck(load().sph_set_variant(self.h, density, forces))
+
+    def variant(self):
+        v = np.zeros(2, np.int32)
+        self._ck(load().sph_get_variant(self.h, _p(v, ctypes.c_int32)))
+        return int(v[0]), int(v[1])
+
+    def autotune(self, reps=3):
+        self._ck(load().sph_autotune(self.h, reps))
+        return self.variant()
 
     def pass_times(self):
         ms = np.zeros(5, np.float64)

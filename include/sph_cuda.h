@@ -139,6 +139,24 @@ int sph_pass_forces(sph_ctx *ctx);
  * collisions and integrate are fused into forces and report 0. */
 int sph_pass_times(sph_ctx *ctx, double ms[5]);
 
+/* Launch variants of the two neighbour passes. Every variant computes the same bits; only
+ * the speed differs (no reference counterpart: the OpenCL kernels have fixed launch shapes,
+ * src/CGPUParticleSimulator.cpp:141-173).
+ *   density: 0 = one particle per thread; 1, 2, 4 = branchless blocked walk with that many
+ *            consecutive sorted particles per thread sharing one candidate scan
+ *   forces:  0 = pair terms inside the candidate loop; 1, 2 = accepted neighbours compacted
+ *            into a per-thread list of 32 / 64 entries in shared memory, pair terms after */
+int sph_set_variant(sph_ctx *ctx, int32_t density_variant, int32_t forces_variant);
+int sph_get_variant(const sph_ctx *ctx, int32_t out[2]);
+
+/* Autotuner: one step in which every density variant and every force variant is timed on the
+ * current state (the density pass is repeated, the force pass re-run from the same inputs),
+ * the fastest of each is kept, and the choice is written to the cache file (SPH_TUNE_CACHE,
+ * else $HOME/.cache/sph_gb300/tune.txt) under the device name, precision and particle-count
+ * bucket (floor(log2 n)). sph_upload applies a cached choice for its bucket. The simulation
+ * advances by exactly one step; reps = timed repetitions per variant (>= 1). */
+int sph_autotune(sph_ctx *ctx, int32_t reps);
+
 /* Particle count of every scene (n_scenes entries). */
 int sph_get_counts(const sph_ctx *ctx, uint32_t *counts);
 uint32_t sph_num_scenes(const sph_ctx *ctx);

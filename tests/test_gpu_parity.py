@@ -356,3 +356,61 @@ def test_full_size_1m_properties(sphlib):
     np.testing.assert_allclose(s["rho_mean"], d["rho"].astype(np.float64).mean(), rtol=1e-9)
     ctx64.close()
     ctx.close()
+
+
+# ------------------------------------------------------------------------- launch variants
+def test_variants_bit_identical(sphlib, oracle_mod):
+    """Every launch variant of the two neighbour passes computes the same bits."""
+    for box, pos, vel, g in [scenes(sphlib, oracle_mod)["c0_8000_moving"],
+                             scenes(sphlib, oracle_mod)["outside_walls"]]:
+        base = None
+        for dv in (0, 1, 2, 4):
+            for fv in (0, 1, 2):
+                ctx = sphlib.SphContext(box, pos.shape[0], gravity=g, flags=2)
+                ctx.set_variant(dv, fv)
+                ctx.upload(pos, vel)
+                ctx.step(6)
+                out = ctx.download(acc=True)
+                ctx.close()
+                if base is None:
+                    base = out
+                for k in out:
+                    assert np.array_equal(out[k], base[k]), (dv, fv, k)
+
+
+def test_autotune_is_one_plain_step(sphlib, tmp_path, monkeypatch):
+    monkeypatch.setenv("SPH_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    pos = c0_scene(sphlib)
+    a = sphlib.SphContext(C0_BOX, pos.shape[0], gravity=G981, flags=2)
+    a.upload(pos)
+    dv, fv = a.autotune(reps=2)
+    assert dv in (0, 1, 2, 4) and fv in (0, 1, 2)
+    a.step(3)
+    b = gpu_run(sphlib, C0_BOX, pos, steps=4, gravity=G981)
+    got = a.download(acc=True)
+    for k in got:
+        assert np.array_equal(got[k], b[k]), k
+    line = (tmp_path / "tune.txt").read_text().strip().splitlines()[-1]
+    assert line.endswith(f" {dv} {fv}") and "|b12" in line  # 8000 particles -> bucket 12
+    # a new context of the same bucket picks the cached variants at upload
+    c = sphlib.SphContext(C0_BOX, pos.shape[0], gravity=G981)
+    c.upload(pos)
+    assert c.variant() == (dv, fv)
+    a.close()
+    c.close()
+
+
+def test_upload_step_download_equals_resident(sphlib):
+    """Stepping through host buffers (upload, step, download each step) reproduces the
+    device-resident run bit for bit: the canonical sort makes the layout irrelevant."""
+    pos = c0_scene(sphlib, dims=(12, 12, 12))
+    ref = gpu_run(sphlib, C0_BOX, pos, steps=8, gravity=G981)
+    ctx = sphlib.SphContext(C0_BOX, pos.shape[0], gravity=G981)
+    x, v = pos, np.zeros_like(pos)
+    for _ in range(8):
+        ctx.upload(x, v)
+        ctx.step(1)
+        d = ctx.download()
+        x, v = d["pos"], d["vel"]
+    assert np.array_equal(x, ref["pos"]) and np.array_equal(v, ref["vel"])
+    ctx.close()
