@@ -219,6 +219,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-budget", type=float, default=90.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--variant", default=None, help="pin launch variants 'density,forces' instead of autotuning")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -243,7 +244,12 @@ def main():
     ctx = sphcuda.SphContext(BOX, N, precision=form, gravity=GRAVITY)
     ctx.upload(pos)
     # one untimed step picks the launch variants (all variants compute the same bits)
-    variant = ctx.autotune(reps=3)
+    if args.variant:
+        ctx.set_variant(*[int(v) for v in args.variant.split(",")])
+        ctx.step(1)
+        variant = ctx.variant()
+    else:
+        variant = ctx.autotune(reps=3)
     ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -356,7 +362,8 @@ def main():
         "e2e": e2e,
         "cpu_baseline": cpu,
         "gpu_launches": KERNELS_PER_STEP * args.steps,
-        "launch_variant": {"density": variant[0], "forces": variant[1], "picked_by": "sph_autotune"},
+        "launch_variant": {"density": variant[0], "forces": variant[1],
+                           "picked_by": "--variant" if args.variant else "sph_autotune"},
         "clocks": clk,
         "wall_s_timed_region": t_wall,
     }

@@ -187,6 +187,7 @@ int allocate(sph_ctx *c)
         {(void **) &b.st_acc64, rs == 8 && rec ? 24 * N : 0},
         {(void **) &b.stats, 64 * c->sc.size()},
         {(void **) &b.stats_partial, 6 * 8 * 64 * c->sc.size()},
+        {(void **) &b.masks, 4 * 36 * N},
     };
     size_t total = 0;
     for (auto &it : items) total += (it.bytes + 255) & ~size_t(255);
@@ -374,7 +375,7 @@ int build_graph(sph_ctx *c, int steps)
 }
 
 bool valid_density(int v) { return v == 0 || v == 1 || v == 2 || v == 4; }
-bool valid_forces(int v) { return v >= 0 && v <= 2; }
+bool valid_forces(int v) { return v >= 0 && v <= 4; }
 
 int bucket_of(uint64_t n)
 {
@@ -709,52 +710,43 @@ int sph_autotune(sph_ctx *c, int32_t reps)
     drop_graph(c);
     int rc = pass_grid(c);
     if (rc) return rc;
-    const int dvs[4] = {0, 1, 2, 4};
+    // every (density, forces) pair, timed as density + forces on the same sorted state; the
+    // mask-driven force pass (3) brings its own density pass
+    struct Cfg { int d, f; };
+    std::vector<Cfg> cfgs;
+    for (int d : {0, 1, 2, 4})
+        for (int f = 0; f <= 2; f++) cfgs.push_back({d, f});
+    cfgs.push_back({0, 3});
+    cfgs.push_back({0, 4});
     float best = 1e30f;
-    int bd = c->tune.density_p;
-    for (int dv : dvs) {
-        c->tune.density_p = dv;
+    int bd = c->tune.density_p, bf = c->tune.forces_mode;
+    for (const Cfg &g : cfgs) {
+        c->tune.density_p = g.d;
+        c->tune.forces_mode = g.f;
         for (int r = 0; r <= reps; r++) {  // the first run is a warm-up
+            CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));  // the force pass adds to the counts
             CK(c, cudaEventRecord(c->ev[0], c->stream));
             c->state = SORTED;
             rc = pass_density(c);
+            if (!rc) rc = pass_forces(c);
             if (rc) return rc;
             CK(c, cudaEventRecord(c->ev[1], c->stream));
             CK(c, cudaEventSynchronize(c->ev[1]));
             const float ms = elapsed(c->ev[0], c->ev[1]);
             if (r > 0 && ms < best) {
                 best = ms;
-                bd = dv;
+                bd = g.d;
+                bf = g.f;
             }
         }
     }
+    // the step itself, with the chosen variants (every variant computes the same bits)
     c->tune.density_p = bd;
-    c->state = SORTED;
-    rc = pass_density(c);
-    if (rc) return rc;
-    best = 1e30f;
-    int bf = c->tune.forces_mode;
-    for (int fv = 0; fv <= 2; fv++) {
-        c->tune.forces_mode = fv;
-        for (int r = 0; r <= reps; r++) {
-            CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));  // the pass adds to the counts
-            CK(c, cudaEventRecord(c->ev[2], c->stream));
-            c->state = DENSE;
-            rc = pass_forces(c);
-            if (rc) return rc;
-            CK(c, cudaEventRecord(c->ev[3], c->stream));
-            CK(c, cudaEventSynchronize(c->ev[3]));
-            const float ms = elapsed(c->ev[2], c->ev[3]);
-            if (r > 0 && ms < best) {
-                best = ms;
-                bf = fv;
-            }
-        }
-    }
     c->tune.forces_mode = bf;
     CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
-    c->state = DENSE;
-    rc = pass_forces(c);
+    c->state = SORTED;
+    rc = pass_density(c);
+    if (!rc) rc = pass_forces(c);
     if (rc) return rc;
     c->tune_pinned = true;
     tune_store(tune_key(c, c->n), bd, bf);

@@ -61,6 +61,7 @@ struct DevBufs {
     double *st_xyz64, *st_vel64, *st_rho64, *st_p64, *st_acc64;
     double *stats;         // per-scene FP64 reductions, 8 doubles each
     double *stats_partial; // per-scene slices of the reductions (kSplit x 6 doubles each)
+    uint32_t *masks;       // accepted-neighbour bit masks of the density pass, 36 words per particle
 };
 
 // ---- exact cell hash -------------------------------------------------------------
@@ -97,10 +98,11 @@ __host__ __device__ inline int cell_axis(double p, float half, float inv_h, doub
 //   density_p : 0 = one particle per thread, first form; 1/2/4 = blocked branchless form
 //               with that many consecutive particles per thread
 //   forces_mode: 0 = pair terms inside the candidate loop; 1/2 = compacted neighbour list
-//               of 32/64 entries per thread in shared memory
+//               of 32/64 entries per thread in shared memory; 3 = driven by the neighbour
+//               masks that the density pass then writes (density_p is ignored)
 struct Tune {
     int density_p = 2;
-    int forces_mode = 2;
+    int forces_mode = 3;
 };
 
 // ---- kernel launchers (sph_kernels.cu) --------------------------------------------

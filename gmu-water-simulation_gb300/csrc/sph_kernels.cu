@@ -301,14 +301,22 @@ __global__ void __launch_bounds__(256) k_rank_permute(const uint2 *__restrict__ 
 // Every density kernel uses this one expression, so all launch variants give the same bits
 // (a candidate outside a particle's own 27 cells is farther than h and adds exactly 0).
 template <class R>
-__device__ __forceinline__ R poly6_term(R dx, R dy, R dz, R h2)
+__device__ __forceinline__ R h2_minus_r2(R dx, R dy, R dz, R h2)
 {
     R t = h2 - dx * dx;
     t -= dy * dy;
     t -= dz * dz;
+    return t;
+}
+template <class R>
+__device__ __forceinline__ R poly6_term(R dx, R dy, R dz, R h2)
+{
+    R t = h2_minus_r2<R>(dx, dy, dz, h2);
     t = t > (R) 0 ? t : (R) 0;
     return t * t * t;
 }
+// Neighbour test shared by every kernel: r^2 < h^2 as h^2 - r^2 > 0 (the reference's r^2 <= h^2
+// differs only for pairs at exactly r = h, whose density and force terms are 0).
 
 // ------------------------------------------------------------------------------------
 // Neighbour walk: the 27 cells around a particle are 9 rows (dy, dz) of 3 cells along x,
@@ -494,9 +502,8 @@ __global__ void __launch_bounds__(256) k_forces(const Vec4<R> *__restrict__ pos,
 #pragma unroll 2
         for (uint32_t j = jb; j < je; j++) {
             const Vec4<R> pj = ld4(pos + j);
-            const R dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            const R r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 <= h2 && j != i) pair_force<R>(pi, vi, qi, j, pos, vel, aux, c, fpx, fpy, fpz, fvx, fvy, fvz);
+            if (h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2) > (R) 0 && j != i)
+                pair_force<R>(pi, vi, qi, j, pos, vel, aux, c, fpx, fpy, fpz, fvx, fvy, fvz);
         }
     });
     finish_particle<R>(i, pi, vi, ai.x, sc, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
@@ -540,13 +547,126 @@ __global__ void __launch_bounds__(BLOCK) k_forces_list(
 #pragma unroll 4
             for (uint32_t j = cb; j < ce; j++) {
                 const Vec4<R> pj = ld4(pos + j);
-                const R dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                const R r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 <= h2 && j != i) list[cnt++][threadIdx.x] = j;
+                if (h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2) > (R) 0 && j != i)
+                    list[cnt++][threadIdx.x] = j;
             }
         }
     });
     drain();
+    finish_particle<R>(i, pi, vi, ai.x, sc, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
+                       cid_out, count);
+}
+
+// ------------------------------------------------------------------------------------
+// Neighbour masks: the density pass already tests every candidate, so it records which ones
+// it accepted. For each particle and each of its 9 rows, the row's candidate window
+// [start of cell x-1, end of cell x+1) is cut into 32-candidate chunks; chunk w of row r is
+// one 32-bit word at masks[(r * MASK_WORDS + w) * n + i] (coalesced across particles). Bit k
+// set = candidate window_start + 32 w + k is a neighbour (self included). Candidates past
+// MASK_WORDS chunks are not recorded: the force pass tests them itself.
+constexpr int MASK_WORDS = 4;
+
+template <class R>
+__global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
+                                                      const uint32_t *__restrict__ start,
+                                                      const SceneDev *__restrict__ scenes, uint32_t n, Consts<R> c,
+                                                      uint32_t *__restrict__ masks)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Vec4<R> pi = ld4(pos + i);
+    const SceneDev sc = load_scene(scenes, wbits(pi.w));
+    int cx, cy, cz;
+    hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
+    const R h2 = c.h2;
+    R acc = 0;
+    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
+    const int xl = cx > 0 ? cx - 1 : 0, xh = cx + 1 < X ? cx + 1 : X - 1;
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; dz++) {
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; dy++) {
+            const int r = (dz + 1) * 3 + (dy + 1);
+            const int z = cz + dz, y = cy + dy;
+            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
+            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
+            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            int w = 0;
+            for (uint32_t cb = jb; cb < je; cb += 32, w++) {
+                // bit k of the chunk's word = candidate cb + k; bits enter at the top and
+                // move down one place per candidate
+                const uint32_t ce = min(je, cb + 32u);
+                uint32_t m = 0;
+#pragma unroll 4
+                for (uint32_t j = cb; j < ce; j++) {
+                    const Vec4<R> pj = ld4(pos + j);
+                    R t = h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
+                    m = (m >> 1) | (t > (R) 0 ? 0x80000000u : 0u);
+                    t = t > (R) 0 ? t : (R) 0;
+                    acc += t * t * t;
+                }
+                m >>= 32 - (ce - cb);
+                if (w < MASK_WORDS) masks[(size_t) (r * MASK_WORDS + w) * n + i] = m;
+            }
+        }
+    }
+    const R rho = rmul(rmul(acc, c.c_poly6), c.mass);
+    const R p = rmul(c.k, rsub(rho, c.rho0));
+    st4(aux + i, Vec4<R>{rho, p, rdiv(p, rmul(rho, rho)), rdiv((R) 1, rho)});
+}
+
+// Forces driven by the density pass's masks: only accepted neighbours are visited, in the
+// same candidate order as the scanning forms (so the sums are bit-identical).
+template <class R, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_forces_mask(
+    const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
+    const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
+    uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, Vec4<R> *__restrict__ pos_out,
+    Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out, uint2 *__restrict__ cid_out,
+    uint32_t *__restrict__ count)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Vec4<R> pi = ld4(pos + i);
+    const Vec4<R> vi = ld4(vel + i);
+    const Vec4<R> ai = ld4(aux + i);
+    const SceneDev sc = load_scene(scenes, wbits(pi.w));
+    int cx, cy, cz;
+    hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
+    const R h2 = c.h2, qi = ai.z;
+    R fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
+    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
+    const int xl = cx > 0 ? cx - 1 : 0, xh = cx + 1 < X ? cx + 1 : X - 1;
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; dz++) {
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; dy++) {
+            const int r = (dz + 1) * 3 + (dy + 1);
+            const int z = cz + dz, y = cy + dy;
+            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
+            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
+            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            const uint32_t nw = (je - jb + 31) / 32;
+            for (uint32_t w = 0; w < nw; w++) {
+                const uint32_t cb = jb + 32 * w;
+                uint32_t m = 0;
+                if (w < (uint32_t) MASK_WORDS) {
+                    m = __ldg(masks + (size_t) (r * MASK_WORDS + w) * n + i);
+                } else {  // beyond the recorded chunks: test the candidates here
+                    const uint32_t ce = min(je, cb + 32u);
+                    for (uint32_t j = ce; j-- > cb;) {
+                        const Vec4<R> pj = ld4(pos + j);
+                        m = (m << 1) | (h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2) > (R) 0 ? 1u : 0u);
+                    }
+                }
+                while (m) {
+                    const uint32_t j = cb + (uint32_t) (__ffs(m) - 1);
+                    m &= m - 1;
+                    if (j != i) pair_force<R>(pi, vi, qi, j, pos, vel, aux, c, fpx, fpy, fpz, fvx, fvy, fvz);
+                }
+            }
+        }
+    }
     finish_particle<R>(i, pi, vi, ai.x, sc, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
                        cid_out, count);
 }
@@ -783,6 +903,10 @@ cudaError_t Launch<R>::density(const DevBufs &b, uint32_t n, Consts<R> c, const 
     if (!n) return cudaSuccess;
     const Vec4<R> *pos = (const Vec4<R> *) b.pos_s;
     Vec4<R> *aux = (Vec4<R> *) b.aux;
+    if (t.forces_mode >= 3) {  // the mask-driven force passes need the masks
+        k_density_mask<R><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c, b.masks);
+        return cudaGetLastError();
+    }
     switch (t.density_p) {
     case 2: k_density_blk<R, 2><<<nblk((n + 1) / 2, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c); break;
     case 4: k_density_blk<R, 4><<<nblk((n + 3) / 4, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c); break;
@@ -800,6 +924,14 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
     const Vec4<R> *pos = (const Vec4<R> *) b.pos_s, *vel = (const Vec4<R> *) b.vel_s, *aux = (const Vec4<R> *) b.aux;
     Vec4<R> *po = (Vec4<R> *) b.pos_u, *vo = (Vec4<R> *) b.vel_u, *ao = record_acc ? (Vec4<R> *) b.acc : nullptr;
     switch (t.forces_mode) {
+    case 3:
+        k_forces_mask<R, 0><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
+                                                          b.masks, po, vo, ao, b.cid_u, b.count);
+        break;
+    case 4:
+        k_forces_mask<R, 4><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
+                                                          b.masks, po, vo, ao, b.cid_u, b.count);
+        break;
     case 1:
         k_forces_list<R, 32, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
                                                                   po, vo, ao, b.cid_u, b.count);

@@ -145,13 +145,15 @@ int sph_pass_times(sph_ctx *ctx, double ms[5]);
  *   density: 0 = one particle per thread; 1, 2, 4 = branchless blocked walk with that many
  *            consecutive sorted particles per thread sharing one candidate scan
  *   forces:  0 = pair terms inside the candidate loop; 1, 2 = accepted neighbours compacted
- *            into a per-thread list of 32 / 64 entries in shared memory, pair terms after */
+ *            into a per-thread list of 32 / 64 entries in shared memory, pair terms after;
+ *            3, 4 = the density pass records each particle's accepted neighbours as bit masks
+ *            per row and the force pass visits only those (density_variant is then unused);
+ *            4 trades registers for occupancy differently from 3 */
 int sph_set_variant(sph_ctx *ctx, int32_t density_variant, int32_t forces_variant);
 int sph_get_variant(const sph_ctx *ctx, int32_t out[2]);
 
-/* Autotuner: one step in which every density variant and every force variant is timed on the
- * current state (the density pass is repeated, the force pass re-run from the same inputs),
- * the fastest of each is kept, and the choice is written to the cache file (SPH_TUNE_CACHE,
+/* Autotuner: one step in which every (density, forces) variant pair is timed on the current
+ * state (both passes re-run from the same sorted inputs), the fastest pair is kept, and the choice is written to the cache file (SPH_TUNE_CACHE,
  * else $HOME/.cache/sph_gb300/tune.txt) under the device name, precision and particle-count
  * bucket (floor(log2 n)). sph_upload applies a cached choice for its bucket. The simulation
  * advances by exactly one step; reps = timed repetitions per variant (>= 1). */
