@@ -309,11 +309,15 @@ __device__ __forceinline__ R h2_minus_r2(R dx, R dy, R dz, R h2)
     return t;
 }
 template <class R>
-__device__ __forceinline__ R poly6_term(R dx, R dy, R dz, R h2)
+__device__ __forceinline__ R poly6_from_t(R t)
 {
-    R t = h2_minus_r2<R>(dx, dy, dz, h2);
     t = t > (R) 0 ? t : (R) 0;
     return t * t * t;
+}
+template <class R>
+__device__ __forceinline__ R poly6_term(R dx, R dy, R dz, R h2)
+{
+    return poly6_from_t<R>(h2_minus_r2<R>(dx, dy, dz, h2));
 }
 // Neighbour test shared by every kernel: r^2 < h^2 as h^2 - r^2 > 0 (the reference's r^2 <= h^2
 // differs only for pairs at exactly r = h, whose density and force terms are 0).
@@ -593,19 +597,32 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
             const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
             int w = 0;
             for (uint32_t cb = jb; cb < je; cb += 32, w++) {
-                // bit k of the chunk's word = candidate cb + k; bits enter at the top and
-                // move down one place per candidate
-                const uint32_t ce = min(je, cb + 32u);
+                // bit k of the chunk's word = candidate cb + k; groups of four unguarded
+                // loads through one base pointer, then a tail
+                const Vec4<R> *pc = pos + cb;
+                const int L = (int) min(je - cb, 32u);
                 uint32_t m = 0;
-#pragma unroll 4
-                for (uint32_t j = cb; j < ce; j++) {
-                    const Vec4<R> pj = ld4(pos + j);
-                    R t = h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
-                    m = (m >> 1) | (t > (R) 0 ? 0x80000000u : 0u);
-                    t = t > (R) 0 ? t : (R) 0;
-                    acc += t * t * t;
+                int k = 0;
+                for (; k + 4 <= L; k += 4) {
+                    const Vec4<R> a0 = ld4(pc + k), a1 = ld4(pc + k + 1), a2 = ld4(pc + k + 2), a3 = ld4(pc + k + 3);
+                    const R t0 = h2_minus_r2<R>(pi.x - a0.x, pi.y - a0.y, pi.z - a0.z, h2);
+                    const R t1 = h2_minus_r2<R>(pi.x - a1.x, pi.y - a1.y, pi.z - a1.z, h2);
+                    const R t2 = h2_minus_r2<R>(pi.x - a2.x, pi.y - a2.y, pi.z - a2.z, h2);
+                    const R t3 = h2_minus_r2<R>(pi.x - a3.x, pi.y - a3.y, pi.z - a3.z, h2);
+                    const uint32_t b4 = (t0 > (R) 0 ? 1u : 0u) | (t1 > (R) 0 ? 2u : 0u) | (t2 > (R) 0 ? 4u : 0u) |
+                                        (t3 > (R) 0 ? 8u : 0u);
+                    m |= b4 << k;
+                    acc += poly6_from_t<R>(t0);
+                    acc += poly6_from_t<R>(t1);
+                    acc += poly6_from_t<R>(t2);
+                    acc += poly6_from_t<R>(t3);
                 }
-                m >>= 32 - (ce - cb);
+                for (; k < L; k++) {
+                    const Vec4<R> a0 = ld4(pc + k);
+                    const R t0 = h2_minus_r2<R>(pi.x - a0.x, pi.y - a0.y, pi.z - a0.z, h2);
+                    m |= (t0 > (R) 0 ? 1u : 0u) << k;
+                    acc += poly6_from_t<R>(t0);
+                }
                 if (w < MASK_WORDS) masks[(size_t) (r * MASK_WORDS + w) * n + i] = m;
             }
         }
@@ -637,35 +654,42 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask(
     R fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
     const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
     const int xl = cx > 0 ? cx - 1 : 0, xh = cx + 1 < X ? cx + 1 : X - 1;
-#pragma unroll 1
-    for (int dz = -1; dz <= 1; dz++) {
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; dy++) {
-            const int r = (dz + 1) * 3 + (dy + 1);
-            const int z = cz + dz, y = cy + dy;
-            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
-            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
-            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
-            const uint32_t nw = (je - jb + 31) / 32;
-            for (uint32_t w = 0; w < nw; w++) {
-                const uint32_t cb = jb + 32 * w;
-                uint32_t m = 0;
+    // One flat loop over this particle's accepted neighbours: each iteration takes one set
+    // bit, refilling the word (next chunk, next row) when it runs empty, so a warp runs for
+    // the largest neighbour count of its lanes rather than the sum of per-word maxima.
+    int rs = 0;                      // next row slot to open, 0..9
+    int r = 0;                       // current row slot
+    uint32_t jb = 0, je = 0, w = 0, nw = 0, m = 0, base = 0;
+    for (;;) {
+        while (m == 0) {
+            if (w < nw) {
+                base = jb + 32 * w;
                 if (w < (uint32_t) MASK_WORDS) {
                     m = __ldg(masks + (size_t) (r * MASK_WORDS + w) * n + i);
                 } else {  // beyond the recorded chunks: test the candidates here
-                    const uint32_t ce = min(je, cb + 32u);
-                    for (uint32_t j = ce; j-- > cb;) {
+                    const uint32_t ce = min(je, base + 32u);
+                    for (uint32_t j = ce; j-- > base;) {
                         const Vec4<R> pj = ld4(pos + j);
                         m = (m << 1) | (h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2) > (R) 0 ? 1u : 0u);
                     }
                 }
-                while (m) {
-                    const uint32_t j = cb + (uint32_t) (__ffs(m) - 1);
-                    m &= m - 1;
-                    if (j != i) pair_force<R>(pi, vi, qi, j, pos, vel, aux, c, fpx, fpy, fpz, fvx, fvy, fvz);
-                }
+                w++;
+                continue;
             }
+            if (rs >= 9) break;
+            r = rs++;
+            const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
+            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
+            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
+            jb = __ldg(start + row + xl);
+            je = __ldg(start + row + xh + 1);
+            nw = (je - jb + 31) / 32;
+            w = 0;
         }
+        if (m == 0) break;
+        const uint32_t j = base + (uint32_t) (__ffs(m) - 1);
+        m &= m - 1;
+        if (j != i) pair_force<R>(pi, vi, qi, j, pos, vel, aux, c, fpx, fpy, fpz, fvx, fvy, fvz);
     }
     finish_particle<R>(i, pi, vi, ai.x, sc, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
                        cid_out, count);
