@@ -87,6 +87,18 @@ int cuda_fail(sph_ctx *c, cudaError_t e, const char *what)
     } while (0)
 
 bool is_f64(const sph_ctx *c) { return c->prm.precision == SPH_F64; }
+bool is_mixed(const sph_ctx *c) { return c->prm.precision == SPH_MIXED; }
+
+MixConsts make_mix(const sph_params &p)
+{
+    MixConsts m{};
+    const double h = (double) p.h, s = h / 16384.0;
+    m.to_units = (float) (16384.0 / h);
+    m.poly6_q = (float) (315.0 / (64.0 * M_PI * std::pow(h, 9)) * std::pow(s, 6));
+    m.spiky_q = (float) (-45.0 / (M_PI * std::pow(h, 6)) * s * s);
+    m.visc_q = (float) (45.0 / (M_PI * std::pow(h, 6)) * s);
+    return m;
+}
 size_t r4_bytes(const sph_ctx *c) { return is_f64(c) ? 32 : 16; }
 
 template <class R>
@@ -163,6 +175,7 @@ void drop_graph(sph_ctx *c)
 int allocate(sph_ctx *c)
 {
     const size_t r4 = r4_bytes(c), rs = is_f64(c) ? 8 : 4;
+    const bool mixed = is_mixed(c);
     const uint64_t N = c->ncap, C = c->ctot;
     const uint64_t nb = (C + 4095) / 4096 + 1;
     uint64_t nobs = 0;
@@ -182,9 +195,11 @@ int allocate(sph_ctx *c)
         {(void **) &b.st_xyz, 12 * N}, {(void **) &b.st_vel, 12 * N},
         {(void **) &b.st_rho, rs == 4 ? 4 * N : 0}, {(void **) &b.st_p, rs == 4 ? 4 * N : 0},
         {(void **) &b.st_acc, rs == 4 && rec ? 12 * N : 0},
-        {(void **) &b.st_xyz64, rs == 8 ? 24 * N : 0}, {(void **) &b.st_vel64, rs == 8 ? 24 * N : 0},
-        {(void **) &b.st_rho64, rs == 8 ? 8 * N : 0}, {(void **) &b.st_p64, rs == 8 ? 8 * N : 0},
-        {(void **) &b.st_acc64, rs == 8 && rec ? 24 * N : 0},
+        {(void **) &b.st_xyz64, (rs == 8 || mixed) ? 24 * N : 0}, {(void **) &b.st_vel64, (rs == 8 || mixed) ? 24 * N : 0},
+        {(void **) &b.st_rho64, (rs == 8 || mixed) ? 8 * N : 0}, {(void **) &b.st_p64, (rs == 8 || mixed) ? 8 * N : 0},
+        {&b.lo_s, mixed ? 16 * N : 0}, {&b.lo_u, mixed ? 16 * N : 0},
+        {(void **) &b.gpos, mixed ? 8 * N : 0}, {(void **) &b.gvel, mixed ? 8 * N : 0},
+        {(void **) &b.st_acc64, (rs == 8 || mixed) && rec ? 24 * N : 0},
         {(void **) &b.stats, 64 * c->sc.size()},
         {(void **) &b.stats_partial, 6 * 8 * 64 * c->sc.size()},
         {(void **) &b.masks, 4 * 36 * N},
@@ -215,8 +230,8 @@ int create_common(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *
     if (!p || !scenes || n_scenes == 0) return fail(nullptr, SPH_ERR_ARG, "params/scenes missing or n_scenes == 0");
     if (p->struct_size != sizeof(sph_params)) return fail(nullptr, SPH_ERR_ARG, "sph_params.struct_size mismatch");
     if (!(p->h > 0) || !(p->dt > 0) || !(p->mass > 0)) return fail(nullptr, SPH_ERR_ARG, "h, dt and mass must be > 0");
-    if (p->precision != SPH_PLAIN_F32 && p->precision != SPH_F64)
-        return fail(nullptr, SPH_ERR_UNSUPPORTED, "precision form not available in this build");
+    if (p->precision != SPH_PLAIN_F32 && p->precision != SPH_F64 && p->precision != SPH_MIXED)
+        return fail(nullptr, SPH_ERR_UNSUPPORTED, "unknown precision form");
     sph_ctx *c = new (std::nothrow) sph_ctx();
     if (!c) return fail(nullptr, SPH_ERR_NOMEM, "host allocation failed");
     c->prm = *p;
@@ -293,20 +308,27 @@ template <class R>
 int run_grid(sph_ctx *c)
 {
     CK(c, Launch<R>::scan(c->b, (uint32_t) c->ctot, c->stream));
-    CK(c, Launch<R>::permute(c->b, c->n, c->stream));
+    if (is_mixed(c)) {
+        CK(c, launch_slot(c->b, c->n, c->stream));
+        CK(c, mixed_permute(c->b, c->n, make_consts<float>(c->prm), make_mix(c->prm), c->stream));
+    } else {
+        CK(c, Launch<R>::permute(c->b, c->n, c->stream));
+    }
     return SPH_OK;
 }
 template <class R>
 int run_density(sph_ctx *c)
 {
-    CK(c, Launch<R>::density(c->b, c->n, make_consts<R>(c->prm), c->tune, c->stream));
+    if (is_mixed(c)) CK(c, mixed_density(c->b, c->n, make_consts<float>(c->prm), make_mix(c->prm), c->stream));
+    else CK(c, Launch<R>::density(c->b, c->n, make_consts<R>(c->prm), c->tune, c->stream));
     return SPH_OK;
 }
 template <class R>
 int run_forces(sph_ctx *c)
 {
-    CK(c, Launch<R>::forces(c->b, c->n, make_consts<R>(c->prm), (c->prm.flags & SPH_FLAG_RECORD_ACC) != 0,
-                            c->tune, c->stream));
+    const bool rec = (c->prm.flags & SPH_FLAG_RECORD_ACC) != 0;
+    if (is_mixed(c)) CK(c, mixed_forces(c->b, c->n, make_consts<float>(c->prm), make_mix(c->prm), rec, c->stream));
+    else CK(c, Launch<R>::forces(c->b, c->n, make_consts<R>(c->prm), rec, c->tune, c->stream));
     return SPH_OK;
 }
 
@@ -527,6 +549,7 @@ int sph_upload(sph_ctx *c, const float *xyz, const float *vel, const uint32_t *c
         if (rc) return rc;
         CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
         if (total) {
+            if (is_mixed(c)) CK(c, cudaMemsetAsync(c->b.lo_u, 0, 16 * total, c->stream));
             CK(c, cudaMemcpyAsync(c->b.st_xyz, xyz, 12 * total, cudaMemcpyHostToDevice, c->stream));
             if (vel) CK(c, cudaMemcpyAsync(c->b.st_vel, vel, 12 * total, cudaMemcpyHostToDevice, c->stream));
             if (is_f64(c))
@@ -564,6 +587,7 @@ int sph_append(sph_ctx *c, uint32_t scene, const float *xyz, const float *vel, u
         return fail(c, SPH_ERR_CAPACITY, "scene " + std::to_string(scene) + " would exceed its capacity");
     CK(c, cudaSetDevice(c->device));
     drop_graph(c);
+    if (is_mixed(c)) CK(c, cudaMemsetAsync((char *) c->b.lo_u + 16ull * c->n, 0, 16ull * n, c->stream));
     CK(c, cudaMemcpyAsync(c->b.st_xyz, xyz, 12ull * n, cudaMemcpyHostToDevice, c->stream));
     if (vel) CK(c, cudaMemcpyAsync(c->b.st_vel, vel, 12ull * n, cudaMemcpyHostToDevice, c->stream));
     if (is_f64(c))
@@ -708,6 +732,7 @@ int sph_autotune(sph_ctx *c, int32_t reps)
     if (c->n == 0) return fail(c, SPH_ERR_STATE, "autotune needs particles");
     CK(c, cudaSetDevice(c->device));
     drop_graph(c);
+    if (is_mixed(c)) return one_step(c);  // one launch form: nothing to choose
     int rc = pass_grid(c);
     if (rc) return rc;
     // every (density, forces) pair, timed as density + forces on the same sorted state; the
@@ -781,7 +806,8 @@ int sph_get_resolution(const sph_ctx *c, uint32_t scene, int32_t res[3])
 static int download_impl(sph_ctx *c, void *xyz, void *vel, void *rho, void *p, void *acc, bool f64)
 {
     if (!c) return SPH_ERR_ARG;
-    if (f64 != is_f64(c)) return fail(c, SPH_ERR_ARG, f64 ? "context is not FP64" : "FP64 context: use sph_download_f64");
+    if (f64 ? !(is_f64(c) || is_mixed(c)) : is_f64(c))
+        return fail(c, SPH_ERR_ARG, f64 ? "context is neither FP64 nor mixed" : "FP64 context: use sph_download_f64");
     if (c->state == EMPTY) return fail(c, SPH_ERR_STATE, "nothing uploaded");
     if (acc && !(c->prm.flags & SPH_FLAG_RECORD_ACC))
         return fail(c, SPH_ERR_STATE, "accelerations need SPH_FLAG_RECORD_ACC");
@@ -806,7 +832,8 @@ static int download_impl(sph_ctx *c, void *xyz, void *vel, void *rho, void *p, v
     // aux records are indexed like the *_u arrays except right after a density pass
     const uint32_t n_aux = c->n_dense;
     const uint32_t n_acc = c->n_forced;
-    if (f64) CK(c, Launch<double>::egress(b, n, n_aux, n_acc, layout_sorted, aux_sorted, c->stream));
+    if (is_mixed(c)) CK(c, mixed_egress(b, n, n_aux, n_acc, layout_sorted, aux_sorted, f64, c->stream));
+    else if (f64) CK(c, Launch<double>::egress(b, n, n_aux, n_acc, layout_sorted, aux_sorted, c->stream));
     else CK(c, Launch<float>::egress(b, n, n_aux, n_acc, layout_sorted, aux_sorted, c->stream));
     if (xyz) CK(c, cudaMemcpyAsync(xyz, sx, 3 * rs * n, cudaMemcpyDeviceToHost, c->stream));
     if (vel) CK(c, cudaMemcpyAsync(vel, sv, 3 * rs * n, cudaMemcpyDeviceToHost, c->stream));

@@ -62,6 +62,10 @@ struct DevBufs {
     double *stats;         // per-scene FP64 reductions, 8 doubles each
     double *stats_partial; // per-scene slices of the reductions (kSplit x 6 doubles each)
     uint32_t *masks;       // accepted-neighbour bit masks of the density pass, 36 words per particle
+    // mixed-precision form only
+    void *lo_s, *lo_u;     // low parts of the hi/lo positions (float4, .w unused)
+    uint2 *gpos;           // gathered positions: 16-bit cell codes x | y << 16, z (sorted order)
+    uint2 *gvel;           // gathered velocities: FP16 x, y, z, 0 (sorted order)
 };
 
 // ---- exact cell hash -------------------------------------------------------------
@@ -94,6 +98,14 @@ __host__ __device__ inline int cell_axis(double p, float half, float inv_h, doub
     return (int) floor(q);
 }
 
+// Constants of the mixed form, whose neighbour displacements are in code units of h / 16384.
+struct MixConsts {
+    float to_units;  // 16384 / h
+    float poly6_q;   // 315 / (64 pi h^9) * (h / 16384)^6: the poly6 factor for (h^2 - r^2) in units^2
+    float spiky_q;   // -45 / (pi h^6) * (h / 16384)^2
+    float visc_q;    // 45 / (pi h^6) * (h / 16384)
+};
+
 // Launch variants of the neighbour kernels (picked per context; see the autotuner).
 //   density_p : 0 = one particle per thread, first form; 1/2/4 = blocked branchless form
 //               with that many consecutive particles per thread
@@ -124,5 +136,16 @@ struct Launch {
                               int aux_sorted, cudaStream_t st);
     static cudaError_t stats(const DevBufs &b, uint32_t nscenes, Consts<R> c, int layout_sorted, cudaStream_t st);
 };
+
+// slot assignment of the counting sort alone (the mixed form has its own permute)
+cudaError_t launch_slot(const DevBufs &b, uint32_t n, cudaStream_t st);
+
+// mixed-precision passes (sph_mixed.cu)
+cudaError_t mixed_permute(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, cudaStream_t st);
+cudaError_t mixed_density(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, cudaStream_t st);
+cudaError_t mixed_forces(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, bool record_acc,
+                         cudaStream_t st);
+cudaError_t mixed_egress(const DevBufs &b, uint32_t n_state, uint32_t n_aux, uint32_t n_acc, int layout_sorted,
+                         int aux_sorted, bool f64, cudaStream_t st);
 
 }  // namespace sph

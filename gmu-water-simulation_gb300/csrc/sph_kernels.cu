@@ -12,105 +12,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "sph_device.cuh"
 #include "sph_internal.h"
 
 namespace sph {
-
-template <class R>
-struct alignas(4 * sizeof(R)) Vec4 {
-    R x, y, z, w;
-};
-
-__device__ __forceinline__ Vec4<float> ld4(const Vec4<float> *p)
-{
-    const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
-    return {v.x, v.y, v.z, v.w};
-}
-__device__ __forceinline__ Vec4<double> ld4(const Vec4<double> *p)
-{
-    const double2 *q = reinterpret_cast<const double2 *>(p);
-    const double2 a = __ldg(q), b = __ldg(q + 1);
-    return {a.x, a.y, b.x, b.y};
-}
-// plain (coherent) loads for buffers written earlier in the same kernel sequence
-__device__ __forceinline__ Vec4<float> ldc4(const Vec4<float> *p)
-{
-    const float4 v = *reinterpret_cast<const float4 *>(p);
-    return {v.x, v.y, v.z, v.w};
-}
-__device__ __forceinline__ Vec4<double> ldc4(const Vec4<double> *p)
-{
-    const double2 *q = reinterpret_cast<const double2 *>(p);
-    const double2 a = q[0], b = q[1];
-    return {a.x, a.y, b.x, b.y};
-}
-__device__ __forceinline__ void st4(Vec4<float> *p, Vec4<float> v)
-{
-    *reinterpret_cast<float4 *>(p) = make_float4(v.x, v.y, v.z, v.w);
-}
-__device__ __forceinline__ void st4(Vec4<double> *p, Vec4<double> v)
-{
-    double2 *q = reinterpret_cast<double2 *>(p);
-    q[0] = make_double2(v.x, v.y);
-    q[1] = make_double2(v.z, v.w);
-}
-// (q, 1/rho) of a neighbour: the upper half of its aux record
-__device__ __forceinline__ void ld_qinv(const Vec4<float> *p, float &q, float &inv)
-{
-    const float2 v = __ldg(reinterpret_cast<const float2 *>(p) + 1);
-    q = v.x;
-    inv = v.y;
-}
-__device__ __forceinline__ void ld_qinv(const Vec4<double> *p, double &q, double &inv)
-{
-    const double2 v = __ldg(reinterpret_cast<const double2 *>(p) + 1);
-    q = v.x;
-    inv = v.y;
-}
-
-// .w fields carry 32-bit integers (scene index in positions, particle id in velocities)
-__device__ __forceinline__ uint32_t wbits(float w) { return __float_as_uint(w); }
-__device__ __forceinline__ uint32_t wbits(double w) { return (uint32_t) __double_as_longlong(w); }
-template <class R>
-__device__ __forceinline__ R mkw(uint32_t v);
-template <>
-__device__ __forceinline__ float mkw<float>(uint32_t v) { return __uint_as_float(v); }
-template <>
-__device__ __forceinline__ double mkw<double>(uint32_t v) { return __longlong_as_double((long long) v); }
-
-// correctly rounded operations that the compiler may not fuse: the per-particle epilogue
-// mirrors the reference's float expression order
-__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
-__device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
-__device__ __forceinline__ float inv_sqrt(float x) { return rsqrtf(x); }
-__device__ __forceinline__ double inv_sqrt(double x) { return 1.0 / sqrt(x); }
-
-template <class R>
-__device__ __forceinline__ uint32_t hash_cell(const SceneDev &sc, R x, R y, R z, const Consts<R> &c, int &cx,
-                                              int &cy, int &cz)
-{
-    cx = cell_axis(x, sc.half[0], c.inv_h_f, c.h_d, sc.res[0]);
-    cy = cell_axis(y, sc.half[1], c.inv_h_f, c.h_d, sc.res[1]);
-    cz = cell_axis(z, sc.half[2], c.inv_h_f, c.h_d, sc.res[2]);
-    return sc.cell_base + (uint32_t) cx + (uint32_t) cy * (uint32_t) sc.res[0] +
-           (uint32_t) cz * (uint32_t) sc.res[0] * (uint32_t) sc.res[1];
-}
-
-__device__ __forceinline__ SceneDev load_scene(const SceneDev *scenes, uint32_t s)
-{
-    SceneDev sc;
-    const uint4 *src = reinterpret_cast<const uint4 *>(scenes + s);
-    uint4 *dst = reinterpret_cast<uint4 *>(&sc);
-#pragma unroll
-    for (int k = 0; k < (int) (sizeof(SceneDev) / 16); k++) dst[k] = __ldg(src + k);
-    return sc;
-}
 
 // ------------------------------------------------------------------------------------
 // ingest: host-staged float xyz/vel -> *_u records with scene/id bits, plus the hash.
@@ -297,31 +202,6 @@ __global__ void __launch_bounds__(256) k_rank_permute(const uint2 *__restrict__ 
     st4(vel_s + dst, ld4(vel_u + i));
 }
 
-// (h^2 - r^2)^3 for r^2 <= h^2, else 0, branchless: t = h^2 - dx^2 - dy^2 - dz^2 clamped at 0.
-// Every density kernel uses this one expression, so all launch variants give the same bits
-// (a candidate outside a particle's own 27 cells is farther than h and adds exactly 0).
-template <class R>
-__device__ __forceinline__ R h2_minus_r2(R dx, R dy, R dz, R h2)
-{
-    R t = h2 - dx * dx;
-    t -= dy * dy;
-    t -= dz * dz;
-    return t;
-}
-template <class R>
-__device__ __forceinline__ R poly6_from_t(R t)
-{
-    t = t > (R) 0 ? t : (R) 0;
-    return t * t * t;
-}
-template <class R>
-__device__ __forceinline__ R poly6_term(R dx, R dy, R dz, R h2)
-{
-    return poly6_from_t<R>(h2_minus_r2<R>(dx, dy, dz, h2));
-}
-// Neighbour test shared by every kernel: r^2 < h^2 as h^2 - r^2 > 0 (the reference's r^2 <= h^2
-// differs only for pairs at exactly r = h, whose density and force terms are 0).
-
 // ------------------------------------------------------------------------------------
 // Neighbour walk: the 27 cells around a particle are 9 rows (dy, dz) of 3 cells along x,
 // and in (cell, id) order each row is one contiguous range of the sorted arrays.
@@ -374,111 +254,6 @@ __global__ void __launch_bounds__(256) k_density(const Vec4<R> *__restrict__ pos
     const R rho = rmul(rmul(acc, c.c_poly6), c.mass);
     const R p = rmul(c.k, rsub(rho, c.rho0));
     st4(aux + i, Vec4<R>{rho, p, rdiv(p, rmul(rho, rho)), rdiv((R) 1, rho)});
-}
-
-// The two walls of one axis (src/CCollisionGeometry.cpp:117-133 restated per component).
-template <class R>
-__device__ __forceinline__ void wall_axis(R p, R v, R half, const Consts<R> &c, R &acc)
-{
-    R d = radd(rmul(rsub(-half, p), (R) 1), c.wall_r);  // min wall, inverse normal +1
-    if (d > (R) 0) acc = radd(radd(acc, rmul(rmul((R) 1, c.wall_k), d)), rmul((R) 1, rmul(c.wall_damp, rmul(v, (R) 1))));
-    d = radd(rmul(rsub(half, p), (R) -1), c.wall_r);    // max wall, inverse normal -1
-    if (d > (R) 0)
-        acc = radd(radd(acc, rmul(rmul((R) -1, c.wall_k), d)), rmul((R) -1, rmul(c.wall_damp, rmul(v, (R) -1))));
-}
-
-// Per-particle epilogue of the force pass: total acceleration from the summed pressure and
-// viscosity terms (src/CCPUParticleSimulator.cpp:189-193), walls (src/CCollisionGeometry.cpp:117-133),
-// box obstacles, position-Verlet integration (src/CCPUParticleSimulator.cpp:211-229), and the
-// cell hash of the new position for the next step. Float operations are explicitly rounded
-// in the reference's order.
-template <class R>
-__device__ __forceinline__ void finish_particle(uint32_t i, const Vec4<R> &pi, const Vec4<R> &vi, R rho,
-                                                const SceneDev &sc, const ObstacleDev *__restrict__ obstacles,
-                                                const Consts<R> &c, R fpx, R fpy, R fpz, R fvx, R fvy, R fvz,
-                                                Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out,
-                                                Vec4<R> *__restrict__ acc_out, uint2 *__restrict__ cid_out,
-                                                uint32_t *__restrict__ count)
-{
-    const R sp = rmul(-c.mass, rho), sv = rmul(c.mu, c.mass);
-    R ax = rdiv(radd(radd(rmul(fpx, sp), rmul(fvx, sv)), rmul((R) sc.gravity[0], rho)), rho);
-    R ay = rdiv(radd(radd(rmul(fpy, sp), rmul(fvy, sv)), rmul((R) sc.gravity[1], rho)), rho);
-    R az = rdiv(radd(radd(rmul(fpz, sp), rmul(fvz, sv)), rmul((R) sc.gravity[2], rho)), rho);
-
-    // walls at -+box/2 in the order left, bottom, back, right, top, front. Each wall acts on
-    // one component only, so per axis: the min wall (inverse normal +1), then the max wall
-    // (inverse normal -1); d = dot(wall - p, n_inv) + r, a += K n_inv d + damp dot(v, n_inv) n_inv.
-    R wx = 0, wy = 0, wz = 0;
-    wall_axis<R>(pi.x, vi.x, (R) sc.half[0], c, wx);
-    wall_axis<R>(pi.y, vi.y, (R) sc.half[1], c, wy);
-    wall_axis<R>(pi.z, vi.z, (R) sc.half[2], c, wz);
-    // box obstacles: inside the obstacle grown by the particle radius, push out through the
-    // nearest face with the wall spring and damping
-    for (uint32_t o = 0; o < sc.n_obs; o++) {
-        const ObstacleDev ob = obstacles[sc.obs_base + o];
-        const R d0 = radd(rsub(pi.x, (R) ob.lo[0]), c.wall_r), d1 = radd(rsub(pi.y, (R) ob.lo[1]), c.wall_r);
-        const R d2 = radd(rsub(pi.z, (R) ob.lo[2]), c.wall_r), d3 = radd(rsub((R) ob.hi[0], pi.x), c.wall_r);
-        const R d4 = radd(rsub((R) ob.hi[1], pi.y), c.wall_r), d5 = radd(rsub((R) ob.hi[2], pi.z), c.wall_r);
-        if (d0 <= (R) 0 || d1 <= (R) 0 || d2 <= (R) 0 || d3 <= (R) 0 || d4 <= (R) 0 || d5 <= (R) 0) continue;
-        // first face with the smallest penetration, in face order
-        R best = d0;
-        int bf = 0;
-        if (d1 < best) { best = d1; bf = 1; }
-        if (d2 < best) { best = d2; bf = 2; }
-        if (d3 < best) { best = d3; bf = 3; }
-        if (d4 < best) { best = d4; bf = 4; }
-        if (d5 < best) { best = d5; bf = 5; }
-        const R sgn = bf < 3 ? (R) -1 : (R) 1;  // outward normal of the face
-        const R kt = rmul(rmul(sgn, c.wall_k), best);
-        const int a = bf % 3;
-        const R v = a == 0 ? vi.x : (a == 1 ? vi.y : vi.z);
-        const R dt = rmul(sgn, rmul(c.wall_damp, rmul(v, sgn)));
-        if (a == 0) wx = radd(radd(wx, kt), dt);
-        else if (a == 1) wy = radd(radd(wy, kt), dt);
-        else wz = radd(radd(wz, kt), dt);
-    }
-    ax = radd(ax, wx);
-    ay = radd(ay, wy);
-    az = radd(az, wz);
-
-    // x' = x + v dt + (a dt) dt ; v' = (x' - x) / dt
-    const R dt = c.dt;
-    const R nx = radd(radd(pi.x, rmul(vi.x, dt)), rmul(rmul(ax, dt), dt));
-    const R ny = radd(radd(pi.y, rmul(vi.y, dt)), rmul(rmul(ay, dt), dt));
-    const R nz = radd(radd(pi.z, rmul(vi.z, dt)), rmul(rmul(az, dt), dt));
-    const R nvx = rdiv(rsub(nx, pi.x), dt), nvy = rdiv(rsub(ny, pi.y), dt), nvz = rdiv(rsub(nz, pi.z), dt);
-    st4(pos_out + i, Vec4<R>{nx, ny, nz, pi.w});
-    st4(vel_out + i, Vec4<R>{nvx, nvy, nvz, vi.w});
-    if (acc_out) st4(acc_out + i, Vec4<R>{ax, ay, az, (R) 0});
-    int qx, qy, qz;
-    const uint32_t cell = hash_cell<R>(sc, nx, ny, nz, c, qx, qy, qz);
-    atomicAdd(count + cell, 1u);
-    cid_out[i] = make_uint2(cell, wbits(vi.w));
-}
-
-// Pressure and viscosity terms of one accepted neighbour (src/CCPUParticleSimulator.cpp:177-183).
-template <class R>
-__device__ __forceinline__ void pair_force(const Vec4<R> &pi, const Vec4<R> &vi, R qi, uint32_t j,
-                                           const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel,
-                                           const Vec4<R> *__restrict__ aux, const Consts<R> &c, R &fpx, R &fpy,
-                                           R &fpz, R &fvx, R &fvy, R &fvz)
-{
-    const Vec4<R> pj = ld4(pos + j);
-    const Vec4<R> vj = ld4(vel + j);
-    R qj, invj;
-    ld_qinv(aux + j, qj, invj);
-    const R dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-    const R r2 = dx * dx + dy * dy + dz * dz;
-    const R rinv = inv_sqrt(r2);
-    const R hr = c.h - r2 * rinv;
-    const R w = (qi + qj) * (c.c_spiky * hr * hr * rinv);  // (p_i/rho_i^2 + p_j/rho_j^2) grad W
-    fpx += w * dx;
-    fpy += w * dy;
-    fpz += w * dz;
-    const R l = c.c_visc * hr * invj;                      // lap W / rho_j
-    fvx += (vj.x - vi.x) * l;
-    fvy += (vj.y - vi.y) * l;
-    fvz += (vj.z - vi.z) * l;
 }
 
 // Forces, first form: one thread per sorted particle, the pair terms evaluated inside the
@@ -568,7 +343,6 @@ __global__ void __launch_bounds__(BLOCK) k_forces_list(
 // one 32-bit word at masks[(r * MASK_WORDS + w) * n + i] (coalesced across particles). Bit k
 // set = candidate window_start + 32 w + k is a neighbour (self included). Candidates past
 // MASK_WORDS chunks are not recorded: the force pass tests them itself.
-constexpr int MASK_WORDS = 4;
 
 template <class R>
 __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
@@ -597,32 +371,19 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
             const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
             int w = 0;
             for (uint32_t cb = jb; cb < je; cb += 32, w++) {
-                // bit k of the chunk's word = candidate cb + k; groups of four unguarded
-                // loads through one base pointer, then a tail
-                const Vec4<R> *pc = pos + cb;
-                const int L = (int) min(je - cb, 32u);
+                // bit k of the chunk's word = candidate cb + k; bits enter at the top and
+                // move down one place per candidate
+                const uint32_t ce = min(je, cb + 32u);
                 uint32_t m = 0;
-                int k = 0;
-                for (; k + 4 <= L; k += 4) {
-                    const Vec4<R> a0 = ld4(pc + k), a1 = ld4(pc + k + 1), a2 = ld4(pc + k + 2), a3 = ld4(pc + k + 3);
-                    const R t0 = h2_minus_r2<R>(pi.x - a0.x, pi.y - a0.y, pi.z - a0.z, h2);
-                    const R t1 = h2_minus_r2<R>(pi.x - a1.x, pi.y - a1.y, pi.z - a1.z, h2);
-                    const R t2 = h2_minus_r2<R>(pi.x - a2.x, pi.y - a2.y, pi.z - a2.z, h2);
-                    const R t3 = h2_minus_r2<R>(pi.x - a3.x, pi.y - a3.y, pi.z - a3.z, h2);
-                    const uint32_t b4 = (t0 > (R) 0 ? 1u : 0u) | (t1 > (R) 0 ? 2u : 0u) | (t2 > (R) 0 ? 4u : 0u) |
-                                        (t3 > (R) 0 ? 8u : 0u);
-                    m |= b4 << k;
-                    acc += poly6_from_t<R>(t0);
-                    acc += poly6_from_t<R>(t1);
-                    acc += poly6_from_t<R>(t2);
-                    acc += poly6_from_t<R>(t3);
+#pragma unroll 4
+                for (uint32_t j = cb; j < ce; j++) {
+                    const Vec4<R> pj = ld4(pos + j);
+                    R t = h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
+                    m = (m >> 1) | (t > (R) 0 ? 0x80000000u : 0u);
+                    t = t > (R) 0 ? t : (R) 0;
+                    acc += t * t * t;
                 }
-                for (; k < L; k++) {
-                    const Vec4<R> a0 = ld4(pc + k);
-                    const R t0 = h2_minus_r2<R>(pi.x - a0.x, pi.y - a0.y, pi.z - a0.z, h2);
-                    m |= (t0 > (R) 0 ? 1u : 0u) << k;
-                    acc += poly6_from_t<R>(t0);
-                }
+                m >>= 32 - (ce - cb);
                 if (w < MASK_WORDS) masks[(size_t) (r * MASK_WORDS + w) * n + i] = m;
             }
         }
@@ -654,42 +415,35 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask(
     R fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
     const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
     const int xl = cx > 0 ? cx - 1 : 0, xh = cx + 1 < X ? cx + 1 : X - 1;
-    // One flat loop over this particle's accepted neighbours: each iteration takes one set
-    // bit, refilling the word (next chunk, next row) when it runs empty, so a warp runs for
-    // the largest neighbour count of its lanes rather than the sum of per-word maxima.
-    int rs = 0;                      // next row slot to open, 0..9
-    int r = 0;                       // current row slot
-    uint32_t jb = 0, je = 0, w = 0, nw = 0, m = 0, base = 0;
-    for (;;) {
-        while (m == 0) {
-            if (w < nw) {
-                base = jb + 32 * w;
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; dz++) {
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; dy++) {
+            const int r = (dz + 1) * 3 + (dy + 1);
+            const int z = cz + dz, y = cy + dy;
+            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
+            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
+            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            const uint32_t nw = (je - jb + 31) / 32;
+            for (uint32_t w = 0; w < nw; w++) {
+                const uint32_t cb = jb + 32 * w;
+                uint32_t m = 0;
                 if (w < (uint32_t) MASK_WORDS) {
                     m = __ldg(masks + (size_t) (r * MASK_WORDS + w) * n + i);
                 } else {  // beyond the recorded chunks: test the candidates here
-                    const uint32_t ce = min(je, base + 32u);
-                    for (uint32_t j = ce; j-- > base;) {
+                    const uint32_t ce = min(je, cb + 32u);
+                    for (uint32_t j = ce; j-- > cb;) {
                         const Vec4<R> pj = ld4(pos + j);
                         m = (m << 1) | (h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2) > (R) 0 ? 1u : 0u);
                     }
                 }
-                w++;
-                continue;
+                while (m) {
+                    const uint32_t j = cb + (uint32_t) (__ffs(m) - 1);
+                    m &= m - 1;
+                    if (j != i) pair_force<R>(pi, vi, qi, j, pos, vel, aux, c, fpx, fpy, fpz, fvx, fvy, fvz);
+                }
             }
-            if (rs >= 9) break;
-            r = rs++;
-            const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
-            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
-            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
-            jb = __ldg(start + row + xl);
-            je = __ldg(start + row + xh + 1);
-            nw = (je - jb + 31) / 32;
-            w = 0;
         }
-        if (m == 0) break;
-        const uint32_t j = base + (uint32_t) (__ffs(m) - 1);
-        m &= m - 1;
-        if (j != i) pair_force<R>(pi, vi, qi, j, pos, vel, aux, c, fpx, fpy, fpz, fvx, fvy, fvz);
     }
     finish_particle<R>(i, pi, vi, ai.x, sc, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
                        cid_out, count);
@@ -1001,6 +755,13 @@ cudaError_t Launch<R>::stats(const DevBufs &b, uint32_t nscenes, Consts<R> c, in
     k_stats_partial<R><<<nscenes * STATS_SPLIT, STATS_THREADS, 0, st>>>(vel, (const Vec4<R> *) b.aux, b.start, b.scenes,
                                                                         b.stats_partial);
     k_stats_final<<<nscenes, 32, 0, st>>>(b.stats_partial, b.start, b.scenes, (double) c.mass, b.stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_slot(const DevBufs &b, uint32_t n, cudaStream_t st)
+{
+    if (!n) return cudaSuccess;
+    k_slot<<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.cursor, b.tmp);
     return cudaGetLastError();
 }
 

@@ -414,3 +414,83 @@ def test_upload_step_download_equals_resident(sphlib):
         x, v = d["pos"], d["vel"]
     assert np.array_equal(x, ref["pos"]) and np.array_equal(v, ref["vel"])
     ctx.close()
+
+
+# ------------------------------------------------------------------------- mixed precision
+def mixed_vs_f64(sphlib, box, pos, vel=None, steps=1, gravity=G981):
+    m = sphlib.SphContext(box, pos.shape[0], precision=sphlib.SPH_MIXED, flags=2, gravity=gravity)
+    m.upload(pos, vel)
+    m.step(steps)
+    got = m.download(acc=True)
+    got64 = {}
+    L = sphlib.load()
+    n = pos.shape[0]
+    x64 = np.zeros((n, 3))
+    L.sph_download_f64(m.h, sphlib._vp(x64), None, None, None, None)
+    m.close()
+    ref = gpu_run(sphlib, box, pos, vel, steps=steps, precision=sphlib.SPH_F64, gravity=gravity)
+    return got, x64, ref
+
+
+def test_mixed_one_step_vs_f64(sphlib, oracle_mod):
+    """Mixed form, one step from an identical state, against the FP64 run:
+    density within 2e-4 relative, acceleration within 2e-3 of its scale, position within
+    2e-6 m (16-bit cell codes resolve h / 16384 = 2.8e-6 m; FP16 neighbour velocities)."""
+    for name in ("ref_default_0.4", "c0_8000_moving"):
+        box, pos, vel, g = scenes(sphlib, oracle_mod)[name]
+        got, x64, ref = mixed_vs_f64(sphlib, box, pos, vel, gravity=g)
+        scale = oracle_run(oracle_mod, box, pos, vel, gravity=g, mode=oracle_mod.F64)["ascale"]
+        rho_err = np.max(np.abs(got["rho"] - ref["rho"]) / ref["rho"])
+        acc_err = np.max(np.linalg.norm(got["acc"] - ref["acc"], axis=1) / scale)
+        pos_err = np.max(np.abs(x64 - ref["pos"]))
+        assert rho_err < 2e-4 and acc_err < 2e-3 and pos_err < 2e-6, (name, rho_err, acc_err, pos_err)
+
+
+def test_mixed_bands_vs_f64_c0(sphlib):
+    """200 steps of the 8,000-particle dam break: mixed aggregates within the plain form's bands."""
+    pos = c0_scene(sphlib)
+    ctx = {p: sphlib.SphContext(C0_BOX, pos.shape[0], precision=p, gravity=G981) for p in (2, 1)}
+    for c in ctx.values():
+        c.upload(pos)
+    worst = {"mean": 0.0, "max": 0.0, "ke": 0.0}
+    for step in range(200):
+        for c in ctx.values():
+            c.step(1)
+        if step % 10 == 9:
+            s, s64 = ctx[2].stats(), ctx[1].stats()
+            assert s["mass"] == s64["mass"]
+            worst["mean"] = max(worst["mean"], abs(s["rho_mean"] - s64["rho_mean"]) / s64["rho_mean"])
+            worst["max"] = max(worst["max"], abs(s["rho_max"] - s64["rho_max"]) / s64["rho_max"])
+            if s64["kinetic"] > 1e-3:
+                worst["ke"] = max(worst["ke"], abs(s["kinetic"] - s64["kinetic"]) / s64["kinetic"])
+    assert worst["mean"] < 2e-2 and worst["max"] < 2e-1 and worst["ke"] < 3e-1, worst
+
+
+def test_mixed_error_growth_tracks_plain(sphlib):
+    """Over 10 steps the mixed form's max density error against FP64 stays within 10x of the
+    plain FP32 form's (both grow chaotically from their first-step rounding)."""
+    pos = c0_scene(sphlib)
+    ref = gpu_run(sphlib, C0_BOX, pos, steps=10, precision=sphlib.SPH_F64, gravity=G981)
+    plain = gpu_run(sphlib, C0_BOX, pos, steps=10, gravity=G981)
+    mixed, _, _ = mixed_vs_f64(sphlib, C0_BOX, pos, steps=10)
+    ep = np.max(np.abs(plain["rho"] - ref["rho"]) / ref["rho"])
+    em = np.max(np.abs(mixed["rho"] - ref["rho"]) / ref["rho"])
+    assert em < max(10 * ep, 1e-3), (em, ep)
+
+
+def test_mixed_batch_and_append(sphlib):
+    """The mixed form batches scenes and appends emitter particles like the plain form."""
+    dims, boxes = sphlib.batch_plan(3, seed=4, nmin=500, nmax=3000)
+    parts = [sphlib.dam_break_scene(tuple(int(x) for x in d), tuple(float(x) for x in b), seed=s)
+             for s, (d, b) in enumerate(zip(dims, boxes))]
+    counts = [p.shape[0] for p in parts]
+    ctx = sphlib.SphContext(boxes, [c + 100 for c in counts], precision=sphlib.SPH_MIXED, gravity=G981)
+    ctx.upload(np.concatenate(parts), None, counts)
+    ctx.step(5)
+    xyz, vel = sphlib.fountain_emit(seed=1, step=0, n=100, center=(0.0, 0.0, 0.0), radius=0.02, speed=0.5,
+                                    sigma=0.01)
+    ctx.append(1, xyz, vel)
+    ctx.step(5)
+    d = ctx.download()
+    assert ctx.n == sum(counts) + 100 and np.all(np.isfinite(d["pos"])) and np.all(np.isfinite(d["rho"]))
+    ctx.close()
