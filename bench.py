@@ -165,6 +165,40 @@ def cpu_baseline(pos, steps_budget_s=12.0, threads=1):
     return pos.shape[0] * n / el, n, el
 
 
+def fp64_error(sphcuda, ctx, form, N):
+    """Max relative error against FP64 of one step from the timed run's final state: the state
+    (hi + lo positions in double for the mixed form) is uploaded into a fresh context of the
+    measured form and into an FP64 context, each steps once, and density, acceleration and
+    position are compared (acceleration against the largest FP64 acceleration, position in m)."""
+    import ctypes
+
+    L = sphcuda.load()
+    x64 = np.zeros((N, 3))
+    v32 = ctx.download()["vel"]
+    if form == sphcuda.SPH_PLAIN_F32:
+        x64 = ctx.download()["pos"].astype(np.float64)
+    else:
+        L.sph_download_f64(ctx.h, ctypes.c_void_p(x64.ctypes.data), None, None, None, None)
+    x32 = x64.astype(np.float32)
+    out = {}
+    for name, prec in (("form", form), ("f64", sphcuda.SPH_F64)):
+        c = sphcuda.SphContext(BOX, N, precision=prec, gravity=GRAVITY, flags=sphcuda.SPH_FLAG_RECORD_ACC)
+        c.upload(x32, v32)
+        c.step(1)
+        out[name] = c.download(acc=True)
+        if prec != sphcuda.SPH_PLAIN_F32:
+            xx = np.zeros((N, 3))
+            L.sph_download_f64(c.h, ctypes.c_void_p(xx.ctypes.data), None, None, None, None)
+            out[name]["pos"] = xx
+        c.close()
+    a, b = out["form"], out["f64"]
+    amax = float(np.max(np.linalg.norm(b["acc"], axis=1)))
+    return {"after": "one step from the timed run's final state",
+            "rho_max_rel": float(np.max(np.abs(a["rho"] - b["rho"]) / np.abs(b["rho"]))),
+            "acc_max_err_over_max_acc": float(np.max(np.linalg.norm(a["acc"] - b["acc"], axis=1)) / amax),
+            "pos_max_abs_m": float(np.max(np.abs(np.asarray(a["pos"], np.float64) - b["pos"])))}
+
+
 def run_reference(args):
     """--impl reference: the oracle restatement of the reference's CPU step on all cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -214,7 +248,7 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="plain", choices=["plain", "f64"])
+    ap.add_argument("--form", default="plain", choices=["plain", "f64", "mixed"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-budget", type=float, default=90.0)
@@ -233,7 +267,7 @@ def main():
     import sphcuda
 
     sphcuda.load()
-    form = {"plain": sphcuda.SPH_PLAIN_F32, "f64": sphcuda.SPH_F64}[args.form]
+    form = {"plain": sphcuda.SPH_PLAIN_F32, "f64": sphcuda.SPH_F64, "mixed": sphcuda.SPH_MIXED}[args.form]
     rs = 8 if args.form == "f64" else 4
     pos = sphcuda.dam_break_scene(DIMS, BOX, SEED)
     N = pos.shape[0]
@@ -294,6 +328,7 @@ def main():
     stats = ctx.stats()
     assert stats["count"] == N and np.isfinite(stats["rho_mean"])
     resident_final = ctx.download()
+    fp64_check = fp64_error(sphcuda, ctx, form, N)
 
     ab = alg_bytes(N, C, rs)
     peak, peak_src = load_peak()
@@ -352,7 +387,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.form == "f64" else "f32", "data": "synthetic (seeded lattice, no dataset)",
-        "config": workload_desc({"plain": "plain FP32", "f64": "FP64"}[args.form]),
+        "config": workload_desc({"plain": "plain FP32", "f64": "FP64", "mixed": "mixed precision"}[args.form]),
+        "fp64_check": fp64_check,
         "roofline": {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
                      "alg_bytes_per_launch": ab[dom], "launch_ms": dom_ms},
