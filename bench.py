@@ -242,6 +242,103 @@ def run_reference(args):
     return 0
 
 
+def build_config(sphcuda, name, seed=0):
+    """Scenes of the other benchmark configurations: (boxes, positions, counts, capacities,
+    obstacles, emitter or None, description)."""
+    if name == "dam8k":
+        box = (1.0, 1.0, 0.5)
+        pos = sphcuda.dam_break_scene((20, 20, 20), box, seed)
+        return [box], pos, [pos.shape[0]], [pos.shape[0]], None, None, (
+            "dam break, 8,000 particles (20^3 lattice), box 1 x 1 x 0.5 m")
+    if name == "batch256":
+        dims, boxes = sphcuda.batch_plan(256, seed=3)
+        parts = [sphcuda.dam_break_scene(tuple(int(x) for x in d), tuple(float(x) for x in b), s)
+                 for s, (d, b) in enumerate(zip(dims, boxes))]
+        counts = [p.shape[0] for p in parts]
+        return list(map(tuple, boxes)), np.concatenate(parts), counts, counts, None, None, (
+            f"256 dam-break scenes, {sum(counts):,} particles, counts log-uniform in [2000, 64000], "
+            "aspect per axis uniform in [0.5, 2], one launch per pass over all scenes")
+    if name == "fountain":
+        box = (2.0, 2.0, 2.0)
+        emit = {"per_step": 2000, "cap": 2_000_000, "center": (0.0, -1.0 + 0.0229, 0.0), "radius": 0.05,
+                "speed": 5.0, "sigma": 0.2}
+        return [box], np.zeros((0, 3), np.float32), [0], [emit["cap"]], None, emit, (
+            "fountain, 2 x 2 x 2 m box, disc emitter r = 0.05 m at the floor centre, 2,000 particles per step at "
+            "5 m/s + N(0, 0.2^2) per component, up to 2,000,000")
+    if name == "dam16m":
+        s_ = 4.57  # box scale: the 400 x 200 x 200 lattice at 0.5h spans 9.14 x 4.57 x 4.57 m
+        box = (4 * s_, s_, s_)
+        pos = sphcuda.dam_break_scene((400, 200, 200), box, seed)
+        rng = np.random.default_rng(seed + 44)
+        obs = []
+        for _ in range(8):
+            size = rng.uniform(0.05, 0.2, 3) * s_
+            c = np.array([rng.uniform(0.05, 0.95) * box[0] / 2, rng.uniform(-0.5, 0.0) * box[1] / 2,
+                          rng.uniform(-0.9, 0.9) * box[2] / 2])
+            obs += list(c - size / 2) + list(c + size / 2)
+        return [box], pos, [pos.shape[0]], [pos.shape[0]], [np.array(obs, np.float32)], None, (
+            "dam break, 16,000,000 particles (400 x 200 x 200 lattice), box 18.28 x 4.57 x 4.57 m (the 4 x 1 x 1 m "
+            "box scaled x4.57 so the lattice fits; it fills the upstream half), 8 seeded box obstacles of "
+            "0.23-0.91 m in the downstream half")
+    raise ValueError(name)
+
+
+def run_config(args):
+    """The other benchmark configurations, timed as replayed whole steps (CUDA graphs) with
+    events on the context's stream; emitter steps append on the host between steps."""
+    import torch
+
+    import sphcuda
+
+    sphcuda.load()
+    form = {"plain": sphcuda.SPH_PLAIN_F32, "f64": sphcuda.SPH_F64, "mixed": sphcuda.SPH_MIXED}[args.form]
+    boxes, pos, counts, caps, obstacles, emit, desc = build_config(sphcuda, args.config)
+    ctx = sphcuda.SphContext(boxes, caps, precision=form, gravity=GRAVITY, obstacles=obstacles)
+    ctx.upload(pos, None, counts)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda:0"))
+    steps_done = [0]
+
+    def advance(k, timed_ms):
+        if emit is None:
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(ext)
+            ctx.step(k)
+            ev1.record(ext)
+            ev1.synchronize()
+            timed_ms.append(ev0.elapsed_time(ev1))
+            return ctx.n * k
+        work = 0
+        for _ in range(k):
+            if ctx.n + emit["per_step"] <= emit["cap"]:
+                xyz, vel = sphcuda.fountain_emit(7, steps_done[0], emit["per_step"], emit["center"], emit["radius"],
+                                                 emit["speed"], emit["sigma"])
+                ctx.append(0, xyz, vel)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(ext)
+            ctx.step(1)
+            ev1.record(ext)
+            ev1.synchronize()
+            timed_ms.append(ev0.elapsed_time(ev1))
+            work += ctx.n
+            steps_done[0] += 1
+        return work
+
+    variant = ctx.autotune(reps=2) if ctx.n else (0, 3)
+    warm = []
+    advance(max(args.warmup, 3), warm)
+    ms = []
+    work = advance(args.steps, ms)
+    st = ctx.stats(0)
+    finite = bool(np.isfinite(st["rho_mean"]))
+    line = {"metric": METRIC, "value": work / (sum(ms) / 1000.0), "unit": UNIT, "config": {"workload": desc,
+            "form": args.form, "particles_final": ctx.n, "scenes": len(boxes)}, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": sum(ms) / args.steps, "launch_variant": list(variant),
+            "finite": finite, "rho_mean_scene0": st["rho_mean"], "l2": "not flushed (replayed steps)"}
+    ctx.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -254,9 +351,13 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=90.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", default=None, help="pin launch variants 'density,forces' instead of autotuning")
+    ap.add_argument("--config", default="dam1m", choices=["dam1m", "dam8k", "batch256", "fountain", "dam16m"],
+                    help="dam1m is the benchmark line; the others are measured separately")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config != "dam1m":
+        return run_config(args)
     if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
         print(json.dumps({"error": "this benchmark runs on one GPU (single-scene path; no multi-GPU path)"}))
         return 2

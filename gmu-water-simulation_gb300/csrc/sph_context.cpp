@@ -92,8 +92,8 @@ bool is_mixed(const sph_ctx *c) { return c->prm.precision == SPH_MIXED; }
 MixConsts make_mix(const sph_params &p)
 {
     MixConsts m{};
-    const double h = (double) p.h, s = h / 16384.0;
-    m.to_units = (float) (16384.0 / h);
+    const double h = (double) p.h, s = h / 8192.0;
+    m.to_units = (float) (8192.0 / h);
     m.poly6_q = (float) (315.0 / (64.0 * M_PI * std::pow(h, 9)) * std::pow(s, 6));
     m.spiky_q = (float) (-45.0 / (M_PI * std::pow(h, 6)) * s * s);
     m.visc_q = (float) (45.0 / (M_PI * std::pow(h, 6)) * s);

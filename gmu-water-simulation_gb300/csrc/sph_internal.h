@@ -64,7 +64,7 @@ struct DevBufs {
     uint32_t *masks;       // accepted-neighbour bit masks of the density pass, 36 words per particle
     // mixed-precision form only
     void *lo_s, *lo_u;     // low parts of the hi/lo positions (float4, .w unused)
-    uint2 *gpos;           // gathered positions: 16-bit cell codes x | y << 16, z (sorted order)
+    uint2 *gpos;           // gathered positions: 16-bit codes x | y << 16, z (sorted order)
     uint2 *gvel;           // gathered velocities: FP16 x, y, z, 0 (sorted order)
 };
 
@@ -98,12 +98,12 @@ __host__ __device__ inline int cell_axis(double p, float half, float inv_h, doub
     return (int) floor(q);
 }
 
-// Constants of the mixed form, whose neighbour displacements are in code units of h / 16384.
+// Constants of the mixed form, whose neighbour displacements are in code units of h / 8192.
 struct MixConsts {
-    float to_units;  // 16384 / h
-    float poly6_q;   // 315 / (64 pi h^9) * (h / 16384)^6: the poly6 factor for (h^2 - r^2) in units^2
-    float spiky_q;   // -45 / (pi h^6) * (h / 16384)^2
-    float visc_q;    // 45 / (pi h^6) * (h / 16384)
+    float to_units;  // 8192 / h
+    float poly6_q;   // 315 / (64 pi h^9) * (h / 8192)^6: the poly6 factor for (h^2 - r^2) in units^2
+    float spiky_q;   // -45 / (pi h^6) * (h / 8192)^2
+    float visc_q;    // 45 / (pi h^6) * (h / 8192)
 };
 
 // Launch variants of the neighbour kernels (picked per context; see the autotuner).

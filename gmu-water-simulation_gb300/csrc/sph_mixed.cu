@@ -2,9 +2,11 @@
 //
 // Same method and pass structure as the plain form (sph_kernels.cu), with these changes:
 //  - neighbour positions are gathered as 16-bit codes per axis (8 bytes per particle instead
-//    of 16): code = (cell mod 4) << 14 | q, q = offset inside the cell in units of h / 16384.
-//    For two particles at most one cell apart along an axis, the 16-bit two's-complement
-//    difference of their codes is their displacement in those units, exactly;
+//    of 16): code = (c mod 8) << 13 | q, where c = floor((p + box/2) / h) is the particle's
+//    unclamped cell along that axis and q its offset inside that cell in units of h / 8192.
+//    The 16-bit two's-complement difference of two codes is the displacement in those units,
+//    exactly, whenever the particles are less than 7 h apart along the axis (every neighbour
+//    candidate is, unless a particle has been pushed more than ~5 h outside the box);
 //  - neighbour velocities are gathered in FP16 (8 bytes instead of 16);
 //  - density sums are compensated (Kahan) FP32 sums;
 //  - each particle's position is a hi/lo FP32 pair through the integration (TwoSum), and the
@@ -19,17 +21,18 @@
 
 namespace sph {
 
-constexpr float QUNITS = 16384.0f;       // code units per h
-constexpr float QH2 = 268435456.0f;      // h^2 in code units^2 (2^28)
+constexpr float QUNITS = 8192.0f;        // code units per h
+constexpr float QH2 = 67108864.0f;       // h^2 in code units^2 (2^26)
 
 // ---- encoding ------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t axis_code(float p, float lo, float half, int cell, float h, float to_units)
+// code of one axis from the hi/lo coordinate: unclamped cell c and offset q inside it
+__device__ __forceinline__ uint32_t axis_code(float p, float lo, float half, float h, float inv_h, float to_units)
 {
-    // offset of the particle inside its cell: p + lo - (cell origin), origin = -half + cell * h
-    const float o = fmaf(-(float) cell, h, p + half) + lo;
-    int q = __float2int_rn(o * to_units);
-    q = q < 0 ? 0 : (q > 16383 ? 16383 : q);
-    return ((uint32_t) (cell & 3) << 14) | (uint32_t) q;
+    const float t = (p + half) + lo;            // distance from the box's min wall
+    const float c = floorf(t * inv_h);
+    int q = __float2int_rd(fmaf(-c, h, t) * to_units);
+    q = q < 0 ? 0 : (q > 8191 ? 8191 : q);      // rounding at a cell face
+    return ((uint32_t) ((int) c & 7) << 13) | (uint32_t) q;
 }
 
 // displacement i - j in code units from the packed codes (x | y << 16, z)
@@ -76,12 +79,9 @@ __global__ void __launch_bounds__(256) k_rank_permute_mixed(
     st4(lo_s + dst, lo);
     st4(vel_s + dst, v);
     const SceneDev sc = load_scene(scenes, wbits(p.w));
-    const uint32_t local = cd.x - sc.cell_base;
-    const uint32_t X = (uint32_t) sc.res[0], XY = X * (uint32_t) sc.res[1];
-    const int cz = (int) (local / XY), cy = (int) ((local % XY) / X), cx = (int) (local % X);
-    const uint32_t qx = axis_code(p.x, lo.x, sc.half[0], cx, c.h, mc.to_units);
-    const uint32_t qy = axis_code(p.y, lo.y, sc.half[1], cy, c.h, mc.to_units);
-    const uint32_t qz = axis_code(p.z, lo.z, sc.half[2], cz, c.h, mc.to_units);
+    const uint32_t qx = axis_code(p.x, lo.x, sc.half[0], c.h, c.inv_h_f, mc.to_units);
+    const uint32_t qy = axis_code(p.y, lo.y, sc.half[1], c.h, c.inv_h_f, mc.to_units);
+    const uint32_t qz = axis_code(p.z, lo.z, sc.half[2], c.h, c.inv_h_f, mc.to_units);
     gpos[dst] = make_uint2(qx | (qy << 16), qz);
     gvel[dst] = pack_half3(v.x, v.y, v.z);
 }
@@ -197,7 +197,9 @@ __global__ void __launch_bounds__(256, 4) k_forces_mixed(
                     code_delta(gi, __ldg(gpos + j), dx, dy_, dz_);
                     unpack_half3(__ldg(gvel + j), vjx, vjy, vjz);
                     const float2 qa = __ldg(reinterpret_cast<const float2 *>(aux + j) + 1);
-                    const float r2 = dx * dx + dy_ * dy_ + dz_ * dz_;
+                    // at least one unit apart: two particles sharing a code (closer than the
+                    // 5.6 um resolution) get no pressure direction rather than a 0/0
+                    const float r2 = fmaxf(dx * dx + dy_ * dy_ + dz_ * dz_, 1.0f);
                     const float rinv = rsqrtf(r2);
                     const float hr = QUNITS - r2 * rinv;
                     const float wgt = (qi + qa.x) * (mc.spiky_q * hr * hr * rinv);

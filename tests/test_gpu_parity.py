@@ -433,17 +433,19 @@ def mixed_vs_f64(sphlib, box, pos, vel=None, steps=1, gravity=G981):
 
 
 def test_mixed_one_step_vs_f64(sphlib, oracle_mod):
-    """Mixed form, one step from an identical state, against the FP64 run:
-    density within 2e-4 relative, acceleration within 2e-3 of its scale, position within
-    2e-6 m (16-bit cell codes resolve h / 16384 = 2.8e-6 m; FP16 neighbour velocities)."""
-    for name in ("ref_default_0.4", "c0_8000_moving"):
+    """Mixed form, one step from an identical state, against the FP64 run: density within
+    1e-3 relative, acceleration within 2e-3 of its scale A, position within 4 ulp + 2e-3 A dt^2
+    (positions are gathered at h / 8192 = 5.6 um resolution, neighbour velocities in FP16)."""
+    for name in ("ref_default_0.4", "c0_8000_moving", "outside_walls"):
         box, pos, vel, g = scenes(sphlib, oracle_mod)[name]
         got, x64, ref = mixed_vs_f64(sphlib, box, pos, vel, gravity=g)
         scale = oracle_run(oracle_mod, box, pos, vel, gravity=g, mode=oracle_mod.F64)["ascale"]
         rho_err = np.max(np.abs(got["rho"] - ref["rho"]) / ref["rho"])
         acc_err = np.max(np.linalg.norm(got["acc"] - ref["acc"], axis=1) / scale)
-        pos_err = np.max(np.abs(x64 - ref["pos"]))
-        assert rho_err < 2e-4 and acc_err < 2e-3 and pos_err < 2e-6, (name, rho_err, acc_err, pos_err)
+        bound = 4 * np.spacing(np.abs(ref["pos"]).astype(np.float32)).astype(np.float64) + \
+            (2e-3 * scale * 1e-4)[:, None]
+        pos_err = np.max(np.abs(x64 - ref["pos"]) / bound)
+        assert rho_err < 1e-3 and acc_err < 2e-3 and pos_err <= 1.0, (name, rho_err, acc_err, pos_err)
 
 
 def test_mixed_bands_vs_f64_c0(sphlib):
@@ -466,16 +468,17 @@ def test_mixed_bands_vs_f64_c0(sphlib):
     assert worst["mean"] < 2e-2 and worst["max"] < 2e-1 and worst["ke"] < 3e-1, worst
 
 
-def test_mixed_error_growth_tracks_plain(sphlib):
-    """Over 10 steps the mixed form's max density error against FP64 stays within 10x of the
-    plain FP32 form's (both grow chaotically from their first-step rounding)."""
+def test_mixed_ten_steps_vs_f64(sphlib):
+    """After 10 steps of the 8,000-particle dam break the mixed form's densities stay within
+    1e-2 of the FP64 run per particle and its mean density within 1e-4 (the flow amplifies any
+    first-step difference, the plain form's included)."""
     pos = c0_scene(sphlib)
     ref = gpu_run(sphlib, C0_BOX, pos, steps=10, precision=sphlib.SPH_F64, gravity=G981)
-    plain = gpu_run(sphlib, C0_BOX, pos, steps=10, gravity=G981)
     mixed, _, _ = mixed_vs_f64(sphlib, C0_BOX, pos, steps=10)
-    ep = np.max(np.abs(plain["rho"] - ref["rho"]) / ref["rho"])
     em = np.max(np.abs(mixed["rho"] - ref["rho"]) / ref["rho"])
-    assert em < max(10 * ep, 1e-3), (em, ep)
+    assert em < 1e-2, em
+    assert abs(mixed["rho"].astype(np.float64).mean() - ref["rho"].mean()) / ref["rho"].mean() < 1e-4
+    assert np.all(np.isfinite(mixed["pos"]))
 
 
 def test_mixed_batch_and_append(sphlib):
