@@ -184,6 +184,25 @@ int sph_get_grid(sph_ctx *ctx, uint32_t *cell_of_particle, uint32_t *cell_counts
  * out[4] kinetic energy, out[5] mean density, out[6] max density, out[7] particle count. */
 int sph_stats(sph_ctx *ctx, uint32_t scene, double out[8]);
 
+/* Grid build that allocates no device memory. No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc once they are running, such as a host application whose
+ * GPU memory is already owned by its own pool allocator, or a per-frame real-time callback
+ * where an allocation's implicit device synchronisation would stall the frame.
+ * Every array is the caller's device memory:
+ *   xyz        3 floats per particle, id order (n particles)
+ *   out_cell   n: cell of each particle, x + y*X + z*X*Y with (X, Y, Z) = ceil(box / h)
+ *   out_start  X*Y*Z + 1: cell starts, out_start[X*Y*Z] = n
+ *   out_order  n: particle ids in ascending (cell, id) order
+ * The cells and order equal the grid that sph_pass_grid builds for the same positions and h.
+ * Working memory is one fixed device array of about 12 MiB inside this library, held by every
+ * GPU that loads it until the process exits, so n and X*Y*Z are each limited to 1,048,576;
+ * larger requests return SPH_ERR_CAPACITY. The first call on a device looks up that array's
+ * device address (make that first call before any stream capture). All calls share the array:
+ * calls whose work overlaps on the GPU race on it and must not be issued. Work is queued on
+ * stream (a cudaStream_t; NULL = the legacy default stream); returns a status code only. */
+int sph_grid_build_noalloc(const float *xyz, uint32_t n, const float box[3], float h, uint32_t *out_cell,
+                           uint32_t *out_start, uint32_t *out_order, void *stream);
+
 /* ---- scene generators (host only, no device needed) ---- */
 
 /* The reference's DAM_BREAK lattice for a cubic box (src/CBaseParticleSimulator.cpp:38-58).
