@@ -208,9 +208,17 @@ def run_reference(args):
     from oracle import oracle as O
 
     O.build()
-    pos = sphcuda.dam_break_scene(DIMS, BOX, SEED)
-    threads = os.cpu_count() or 1
-    o = O.Oracle(BOX, O.REF, threads=threads, gravity=GRAVITY)
+    threads = args.threads or os.cpu_count() or 1
+    if args.config == "dam1m":
+        box, pos, obstacles, desc = BOX, sphcuda.dam_break_scene(DIMS, BOX, SEED), None, None
+    else:
+        boxes, pos, counts, caps, obs, emit, desc = build_config(sphcuda, args.config)
+        if len(boxes) != 1 or emit is not None:
+            print(json.dumps({"impl": "reference", "unavailable": f"config {args.config}: the oracle runs one "
+                              "scene without emitters"}))
+            return 0
+        box, obstacles = boxes[0], (obs[0] if obs else None)
+    o = O.Oracle(box, O.REF, threads=threads, gravity=GRAVITY, obstacles=obstacles)
     o.add(pos)
     warm = min(args.warmup, 3)
     for _ in range(warm):
@@ -225,6 +233,10 @@ def run_reference(args):
             break
     el = time.perf_counter() - t0
     value = pos.shape[0] * done / el
+    if desc is not None:
+        print(json.dumps({"impl": "reference", "config": {"workload": desc}, "value": value, "unit": UNIT,
+                          "steps": done, "cores": threads, "ms_per_step": 1000 * el / done}), flush=True)
+        return 0
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": done,
         "warmup": warm, "ms_per_step": 1000 * el / done, "higher_is_better": True,
@@ -349,6 +361,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-budget", type=float, default=90.0)
+    ap.add_argument("--threads", type=int, default=0, help="host threads of the reference arm (0 = all)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", default=None, help="pin launch variants 'density,forces' instead of autotuning")
     ap.add_argument("--config", default="dam1m", choices=["dam1m", "dam8k", "batch256", "fountain", "dam16m"],

@@ -8,7 +8,8 @@
 //    exactly, whenever the particles are less than 7 h apart along the axis (every neighbour
 //    candidate is, unless a particle has been pushed more than ~5 h outside the box);
 //  - neighbour velocities are gathered in FP16 (8 bytes instead of 16);
-//  - density sums are compensated (Kahan) FP32 sums;
+//  - density sums are compensated FP32 sums: each 32-candidate chunk is summed, and the chunk
+//    sums are added with Kahan compensation;
 //  - each particle's position is a hi/lo FP32 pair through the integration (TwoSum), and the
 //    velocity update is the increment over dt, so no cancellation of x' - x occurs.
 // The master state (hi, lo, FP32 velocity) is still read and written once per pass.
@@ -126,14 +127,16 @@ __global__ void __launch_bounds__(256) k_density_mixed(const Vec4<float> *__rest
                 // bit k of the chunk's word = candidate cb + k (bits enter at the top)
                 const uint32_t ce = min(je, cb + 32u);
                 uint32_t m = 0;
+                float csum = 0.0f;  // the chunk's terms (at most 32), then one compensated add
 #pragma unroll 4
                 for (uint32_t j = cb; j < ce; j++) {
                     float x, yy, zz;
                     code_delta(gi, __ldg(gpos + j), x, yy, zz);
                     const float t = h2_minus_r2<float>(x, yy, zz, QH2);
                     m = (m >> 1) | (t > 0.0f ? 0x80000000u : 0u);
-                    kahan_add(sum, comp, poly6_from_t<float>(t));
+                    csum += poly6_from_t<float>(t);
                 }
+                kahan_add(sum, comp, csum);
                 m >>= 32 - (ce - cb);
                 if (w < MASK_WORDS) masks[(size_t) (r * MASK_WORDS + w) * n + i] = m;
             }

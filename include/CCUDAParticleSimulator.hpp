@@ -1,0 +1,178 @@
+// CCUDAParticleSimulator.hpp -- Qt-free C++ mirror of the reference's simulator interface
+// (CBaseParticleSimulator, include/CBaseParticleSimulator.h:29-110) for the CUDA step.
+//
+// Same method names and meaning as the reference: the constructor takes the cubic box size
+// and the scenario; setupScene() adds the scenario's particles
+// (src/CBaseParticleSimulator.cpp:38-65); step() runs generateParticles and the five passes in
+// the reference's order (:116-144); the pass methods return milliseconds (0 when profiling is
+// off, and 0 for updateCollisions/integrate, which are fused into updateForces); a failing
+// step stops the simulator and reports through the errorOccured callback, as
+// CGPUBaseParticleSimulator::step does (src/CGPUBaseParticleSimulator.cpp:28-37). The Qt
+// adapter in INTEGRATION.md wraps the same calls in a CBaseParticleSimulator subclass.
+#ifndef CCUDAPARTICLESIMULATOR_HPP
+#define CCUDAPARTICLESIMULATOR_HPP
+
+#include <cmath>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "sph_cuda.h"
+
+enum SimulationScenario { DAM_BREAK = 0, FOUNTAIN };  // include/CBaseParticleSimulator.h:21-25
+
+class CCUDAParticleSimulator
+{
+public:
+    struct SphException : std::runtime_error {
+        int code;
+        SphException(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+    };
+
+    explicit CCUDAParticleSimulator(float boxSize, SimulationScenario scenario = DAM_BREAK, bool profiling = true,
+                                    int precision = SPH_PLAIN_F32)
+        : m_boxSize(boxSize), m_scenario(scenario), m_profiling(profiling), m_precision(precision)
+    {
+        m_gravity[0] = 0.0f;
+        m_gravity[1] = -9.80665f;  // GRAVITY_ACCELERATION, include/CBaseParticleSimulator.h:19
+        m_gravity[2] = 0.0f;
+    }
+    ~CCUDAParticleSimulator() { sph_destroy(m_ctx); }
+    CCUDAParticleSimulator(const CCUDAParticleSimulator &) = delete;
+    CCUDAParticleSimulator &operator=(const CCUDAParticleSimulator &) = delete;
+
+    std::function<void(const char *)> errorOccured;  // the errorOccured(const char*) signal
+
+    void setupScene()
+    {
+        const double halfParticle = 0.0457f / 2.0f;
+        const unsigned calculatedCount = (unsigned) (std::ceil(m_boxSize / halfParticle) *
+                                                     std::ceil(m_boxSize / halfParticle) *
+                                                     std::ceil(m_boxSize / 4 / halfParticle));
+        std::vector<float> xyz;
+        if (m_scenario == DAM_BREAK) {
+            const int64_t n = sph_scene_reference_dam_break(m_boxSize, nullptr, 0);
+            xyz.resize(3 * (size_t) n);
+            sph_scene_reference_dam_break(m_boxSize, xyz.data(), (uint64_t) n);
+            if ((unsigned) n != calculatedCount) throw SphException(SPH_ERR_STATE, "scene count mismatch");
+            m_maxParticlesCount = (unsigned) n;
+        } else {
+            m_maxParticlesCount = calculatedCount;
+        }
+        sph_params p;
+        sph_params_default(&p);
+        for (int a = 0; a < 3; a++) p.gravity[a] = m_gravity[a];
+        p.flags = m_profiling ? SPH_FLAG_PROFILE : 0u;
+        p.precision = m_precision;
+        const float box[3] = {m_boxSize, m_boxSize, m_boxSize};
+        sph_destroy(m_ctx);
+        m_ctx = nullptr;
+        check(sph_create(&p, box, m_maxParticlesCount ? m_maxParticlesCount : 1, &m_ctx), true);
+        const uint32_t count = (uint32_t) (xyz.size() / 3);
+        check(sph_upload(m_ctx, xyz.data(), nullptr, &count));
+        m_particlesCount = count;
+    }
+
+    void setGravityVector(const float g[3])
+    {
+        for (int a = 0; a < 3; a++) m_gravity[a] = g[a];
+        if (m_ctx) check(sph_set_gravity(m_ctx, -1, m_gravity));
+    }
+
+    std::string getSelectedDevice() const { return m_ctx ? sph_device_name(m_ctx) : std::string(); }
+
+    void step()
+    {
+        try {
+            generateParticles();
+            m_last[0] = updateGrid();
+            m_last[1] = updateDensityPressure();
+            m_last[2] = updateForces();
+            m_last[3] = updateCollisions();
+            m_last[4] = integrate();
+            ++m_totalIteration;
+        } catch (const SphException &e) {
+            if (errorOccured) errorOccured(e.what());
+            stop();
+        }
+    }
+
+    void start() { m_running = true; }
+    void stop() { m_running = false; }
+    bool isRunning() const { return m_running; }
+
+    unsigned long getParticlesCount() const { return m_particlesCount; }
+    unsigned long getMaxParticlesCount() const { return m_maxParticlesCount; }
+    unsigned long getTotalIteration() const { return m_totalIteration; }
+    const double *lastPassTimes() const { return m_last; }  // grid, density, forces, collisions, integrate
+    sph_ctx *context() { return m_ctx; }
+
+    // id-ordered state, as CGPUBaseParticleSimulator::integrate reads it back
+    void readState(std::vector<float> &xyz, std::vector<float> &vel, std::vector<float> &rho)
+    {
+        xyz.resize(3 * m_particlesCount);
+        vel.resize(3 * m_particlesCount);
+        rho.resize(m_particlesCount);
+        check(sph_download(m_ctx, xyz.data(), vel.data(), rho.data(), nullptr, nullptr));
+    }
+
+    double updateGrid()
+    {
+        check(sph_pass_grid(m_ctx));
+        return 0.0;
+    }
+    double updateDensityPressure()
+    {
+        check(sph_pass_density(m_ctx));
+        return 0.0;
+    }
+    double updateForces()
+    {
+        check(sph_pass_forces(m_ctx));
+        if (!m_profiling) return 0.0;
+        double ms[5];
+        check(sph_pass_times(m_ctx, ms));
+        m_last[0] = ms[0];  // the grid and density passes are timed with the step's events
+        m_last[1] = ms[1];
+        return ms[2];
+    }
+    double updateCollisions() { return 0.0; }  // fused into updateForces
+    double integrate() { return 0.0; }         // fused into updateForces
+
+private:
+    void check(int rc, bool creating = false)
+    {
+        if (rc != SPH_OK) throw SphException(rc, sph_last_error(creating ? nullptr : m_ctx));
+    }
+
+    // FOUNTAIN emitter (src/CBaseParticleSimulator.cpp:187-210): 7 particles per step
+    void generateParticles()
+    {
+        if (m_scenario != FOUNTAIN) return;
+        const unsigned per = 7;
+        if (m_particlesCount >= m_maxParticlesCount - per) return;
+        const float hp = 0.0457f / 2.0f, q = 0.0457f / 4, oy = -m_boxSize / 2.0f;
+        const float pts[21] = {0, oy, 0, -hp, oy, 0, hp, oy, 0, -q, oy, -hp, q, oy, -hp, -q, oy, hp, q, oy, hp};
+        float vel[21];
+        for (unsigned k = 0; k < per; k++) {
+            vel[3 * k] = 0.0f;
+            vel[3 * k + 1] = m_boxSize * 3.2f;
+            vel[3 * k + 2] = 0.0f;
+        }
+        check(sph_append(m_ctx, 0, pts, vel, per));
+        m_particlesCount += per;
+    }
+
+    float m_boxSize;
+    SimulationScenario m_scenario;
+    bool m_profiling;
+    int m_precision;
+    float m_gravity[3];
+    sph_ctx *m_ctx = nullptr;
+    unsigned long m_particlesCount = 0, m_maxParticlesCount = 0, m_totalIteration = 0;
+    bool m_running = false;
+    double m_last[5] = {0, 0, 0, 0, 0};
+};
+
+#endif  // CCUDAPARTICLESIMULATOR_HPP

@@ -497,3 +497,30 @@ def test_mixed_batch_and_append(sphlib):
     d = ctx.download()
     assert ctx.n == sum(counts) + 100 and np.all(np.isfinite(d["pos"])) and np.all(np.isfinite(d["rho"]))
     ctx.close()
+
+
+def test_one_step_with_obstacles_vs_oracle(sphlib, oracle_mod):
+    """Box obstacles (no reference counterpart: nearest-face push-out with the wall constants,
+    restated in the oracle): one plain FP32 step against the oracle, particles inside, beside
+    and straddling two obstacles."""
+    box = (0.6, 0.5, 0.5)
+    obstacles = np.array([[-0.05, -0.25, -0.05, 0.05, -0.1, 0.05],
+                          [0.12, -0.2, -0.2, 0.2, 0.0, -0.1]], np.float32)
+    rng = np.random.default_rng(21)
+    pos = sphlib.dam_break_scene((14, 10, 10), box, seed=8)
+    pos[:, 0] += np.float32(0.22)  # lattice across both obstacles
+    vel = rng.normal(0, 0.3, pos.shape).astype(np.float32)
+    ctx = sphlib.SphContext(box, pos.shape[0], flags=2, gravity=G981, obstacles=[obstacles])
+    ctx.upload(pos, vel)
+    ctx.step(1)
+    got = ctx.download(acc=True)
+    ctx.close()
+    o = oracle_mod.Oracle(box, oracle_mod.REF, threads=os.cpu_count(), gravity=G981, obstacles=obstacles)
+    o.add(pos, vel)
+    o.step(1)
+    ref = o.state()
+    inside = np.zeros(pos.shape[0], bool)
+    for ob in obstacles:
+        inside |= np.all((pos > ob[:3] - 0.01) & (pos < ob[3:] + 0.01), axis=1)
+    assert inside.sum() > 20  # the case exercises the obstacle response
+    assert_within(rel_errors(got, ref), "obstacles")
