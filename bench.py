@@ -78,12 +78,21 @@ def alg_bytes(N, C, rs=4):
         "slot": 12 * N + 8 * C,
         # (cell, id) + the cell's ids read, state read and written in sorted order, starts
         "rank_permute": 8 * N + 4 * N + 4 * r4 * N + 4 * C,
-        # sorted positions read, (rho, p, p/rho^2, 1/rho) written, row starts
-        "density": r4 * N + r4 * N + 4 * C,
+        # sorted positions read, (rho, p, p/rho^2, 1/rho) written, row starts; the mask form
+        # also writes the neighbour masks (one word per row at rest density: 36 B)
+        "density": r4 * N + r4 * N + 4 * C + MASK_BYTES * N,
         # own position, velocity, aux read; new position, velocity, (cell, id) written;
-        # row starts read; counts read-modify-write
-        "forces": 3 * r4 * N + 2 * r4 * N + 8 * N + 12 * C,
+        # row starts read; counts read-modify-write; the mask form reads the masks
+        "forces": 3 * r4 * N + 2 * r4 * N + 8 * N + 12 * C + MASK_BYTES * N,
     }
+
+
+MASK_BYTES = 36  # 9 rows x one 32-bit mask word per particle (rest density)
+
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernels,
+# from one ncu capture of an early step of this workload (L2 flushed before each replay);
+# profiles/step_kernels_dam_break_1m.md
+TRAFFIC = {"k_forces": 102.44e6, "k_density": 21.43e6}
 
 
 def load_peak():
@@ -450,13 +459,7 @@ def main():
     dom = "forces" if mean(forc_ms) >= mean(dens_ms) else "density"
     dom_ms = mean(forc_ms) if dom == "forces" else mean(dens_ms)
     achieved = ab[dom] / (dom_ms / 1000.0) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        try:
-            traffic = json.load(open(tpath)).get(f"k_{dom}", {}).get("bytes_per_launch")
-        except Exception:
-            traffic = None
+    traffic = TRAFFIC.get(f"k_{dom}") if args.form == "plain" and not args.variant else None
     step_bytes = sum(ab.values())
 
     # ---- end to end through the C ABI with pinned host buffers, the same state sequence:
