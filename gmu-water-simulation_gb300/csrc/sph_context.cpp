@@ -397,7 +397,7 @@ int build_graph(sph_ctx *c, int steps)
 }
 
 bool valid_density(int v) { return v == 0 || v == 1 || v == 2 || v == 4; }
-bool valid_forces(int v) { return v >= 0 && v <= 4; }
+bool valid_forces(int v) { return v >= 0 && v <= 6; }
 
 int bucket_of(uint64_t n)
 {
@@ -743,6 +743,8 @@ int sph_autotune(sph_ctx *c, int32_t reps)
         for (int f = 0; f <= 2; f++) cfgs.push_back({d, f});
     cfgs.push_back({0, 3});
     cfgs.push_back({0, 4});
+    cfgs.push_back({0, 5});
+    cfgs.push_back({0, 6});
     float best = 1e30f;
     int bd = c->tune.density_p, bf = c->tune.forces_mode;
     for (const Cfg &g : cfgs) {

@@ -218,6 +218,11 @@ __device__ __forceinline__ void finish_particle(uint32_t i, const Vec4<R> &pi, c
     cid_out[i] = make_uint2(cell, wbits(vi.w));
 }
 
+template <class R>
+__device__ __forceinline__ void pair_terms(const Vec4<R> &pi, const Vec4<R> &vi, R qi, const Vec4<R> &pj,
+                                           const Vec4<R> &vj, R qj, R invj, const Consts<R> &c, R &fpx, R &fpy,
+                                           R &fpz, R &fvx, R &fvy, R &fvz);
+
 // Pressure and viscosity terms of one accepted neighbour (src/CCPUParticleSimulator.cpp:177-183).
 template <class R>
 __device__ __forceinline__ void pair_force(const Vec4<R> &pi, const Vec4<R> &vi, R qi, uint32_t j,
@@ -229,6 +234,15 @@ __device__ __forceinline__ void pair_force(const Vec4<R> &pi, const Vec4<R> &vi,
     const Vec4<R> vj = ld4(vel + j);
     R qj, invj;
     ld_qinv(aux + j, qj, invj);
+    pair_terms<R>(pi, vi, qi, pj, vj, qj, invj, c, fpx, fpy, fpz, fvx, fvy, fvz);
+}
+
+// The same terms from a neighbour's records already loaded (pair_force's arithmetic).
+template <class R>
+__device__ __forceinline__ void pair_terms(const Vec4<R> &pi, const Vec4<R> &vi, R qi, const Vec4<R> &pj,
+                                           const Vec4<R> &vj, R qj, R invj, const Consts<R> &c, R &fpx, R &fpy,
+                                           R &fpz, R &fvx, R &fvy, R &fvz)
+{
     const R dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const R r2 = dx * dx + dy * dy + dz * dz;
     const R rinv = inv_sqrt(r2);

@@ -449,6 +449,74 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask(
                        cid_out, count);
 }
 
+// Forces from the masks, two accepted neighbours per iteration: both neighbours' records are
+// loaded before either's terms are added, so two gathers are in flight at once and the loop
+// overhead is paid once per pair. The terms are still added one neighbour at a time in
+// candidate order (the sums are the same bits as the other forms).
+template <class R, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_forces_mask2(
+    const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
+    const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
+    uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, Vec4<R> *__restrict__ pos_out,
+    Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out, uint2 *__restrict__ cid_out,
+    uint32_t *__restrict__ count)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Vec4<R> pi = ld4(pos + i);
+    const Vec4<R> vi = ld4(vel + i);
+    const Vec4<R> ai = ld4(aux + i);
+    const SceneDev sc = load_scene(scenes, wbits(pi.w));
+    int cx, cy, cz;
+    hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
+    const R h2 = c.h2, qi = ai.z;
+    R fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
+    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
+    const int xl = cx > 0 ? cx - 1 : 0, xh = cx + 1 < X ? cx + 1 : X - 1;
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; dz++) {
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; dy++) {
+            const int r = (dz + 1) * 3 + (dy + 1);
+            const int z = cz + dz, y = cy + dy;
+            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
+            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
+            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            const uint32_t nw = (je - jb + 31) / 32;
+            for (uint32_t w = 0; w < nw; w++) {
+                const uint32_t cb = jb + 32 * w;
+                uint32_t m = 0;
+                if (w < (uint32_t) MASK_WORDS) {
+                    m = __ldg(masks + (size_t) (r * MASK_WORDS + w) * n + i);
+                } else {  // beyond the recorded chunks: test the candidates here
+                    const uint32_t ce = min(je, cb + 32u);
+                    for (uint32_t j = ce; j-- > cb;) {
+                        const Vec4<R> pj = ld4(pos + j);
+                        m = (m << 1) | (h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2) > (R) 0 ? 1u : 0u);
+                    }
+                }
+                if (i - cb < 32u) m &= ~(1u << (i - cb));  // the particle itself
+                while (m) {
+                    const uint32_t j0 = cb + (uint32_t) (__ffs(m) - 1);
+                    m &= m - 1;
+                    const bool two = m != 0;
+                    const uint32_t j1 = two ? cb + (uint32_t) (__ffs(m) - 1) : j0;
+                    m &= m - 1;
+                    const Vec4<R> p0 = ld4(pos + j0), v0 = ld4(vel + j0);
+                    const Vec4<R> p1 = ld4(pos + j1), v1 = ld4(vel + j1);
+                    R q0, inv0, q1, inv1;
+                    ld_qinv(aux + j0, q0, inv0);
+                    ld_qinv(aux + j1, q1, inv1);
+                    pair_terms<R>(pi, vi, qi, p0, v0, q0, inv0, c, fpx, fpy, fpz, fvx, fvy, fvz);
+                    if (two) pair_terms<R>(pi, vi, qi, p1, v1, q1, inv1, c, fpx, fpy, fpz, fvx, fvy, fvz);
+                }
+            }
+        }
+    }
+    finish_particle<R>(i, pi, vi, ai.x, sc, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
+                       cid_out, count);
+}
+
 // Density, blocked form: each thread owns P consecutive sorted particles. When they share a
 // scene and a (y, z) row of cells (nearly always in sorted order) one candidate scan over the
 // union x-range serves all of them: a candidate outside a particle's own 3 x 3 x 3 block is
@@ -709,6 +777,14 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
     case 4:
         k_forces_mask<R, 4><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
                                                           b.masks, po, vo, ao, b.cid_u, b.count);
+        break;
+    case 5:
+        k_forces_mask2<R, 4><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
+                                                           b.masks, po, vo, ao, b.cid_u, b.count);
+        break;
+    case 6:
+        k_forces_mask2<R, 0><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
+                                                           b.masks, po, vo, ao, b.cid_u, b.count);
         break;
     case 1:
         k_forces_list<R, 32, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
