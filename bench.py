@@ -219,29 +219,44 @@ def run_reference(args):
     O.build()
     threads = args.threads or os.cpu_count() or 1
     if args.config == "dam1m":
-        box, pos, obstacles, desc = BOX, sphcuda.dam_break_scene(DIMS, BOX, SEED), None, None
+        box, pos, obstacles, desc, emit = BOX, sphcuda.dam_break_scene(DIMS, BOX, SEED), None, None, None
     else:
         boxes, pos, counts, caps, obs, emit, desc = build_config(sphcuda, args.config)
-        if len(boxes) != 1 or emit is not None:
+        if len(boxes) != 1:
             print(json.dumps({"impl": "reference", "unavailable": f"config {args.config}: the oracle runs one "
-                              "scene without emitters"}))
+                              "scene"}))
             return 0
         box, obstacles = boxes[0], (obs[0] if obs else None)
     o = O.Oracle(box, O.REF, threads=threads, gravity=GRAVITY, obstacles=obstacles)
-    o.add(pos)
+    if pos.shape[0]:
+        o.add(pos)
+    emitted = [0]
+
+    def one_step():
+        # the emitter (host generator, the same particles as the device emitter) is the
+        # step's first phase, as generateParticles is in the reference
+        if emit is not None and o.n + emit["per_step"] <= emit["cap"]:
+            xyz, vel = sphcuda.fountain_emit(7, emitted[0], emit["per_step"], emit["center"], emit["radius"],
+                                             emit["speed"], emit["sigma"])
+            o.add(xyz, vel)
+        emitted[0] += 1
+        o.step(1)
+        return o.n
+
     warm = min(args.warmup, 3)
     for _ in range(warm):
-        o.step(1)
-    # each timed step is one full step of the 1M scene; stop at K steps or the time budget
+        one_step()
+    # each timed step is one full step of the scene; stop at K steps or the time budget
     t0 = time.perf_counter()
     done = 0
+    work = 0
     while done < args.steps:
-        o.step(1)
+        work += one_step()
         done += 1
         if time.perf_counter() - t0 > args.ref_budget:
             break
     el = time.perf_counter() - t0
-    value = pos.shape[0] * done / el
+    value = work / el
     if desc is not None:
         print(json.dumps({"impl": "reference", "config": {"workload": desc}, "value": value, "unit": UNIT,
                           "steps": done, "cores": threads, "ms_per_step": 1000 * el / done}), flush=True)
@@ -306,7 +321,7 @@ def build_config(sphcuda, name, seed=0):
 
 def run_config(args):
     """The other benchmark configurations, timed as replayed whole steps (CUDA graphs) with
-    events on the context's stream; emitter steps append on the host between steps."""
+    events on the context's stream; an emitter step times the device emitter and the step."""
     import torch
 
     import sphcuda
@@ -330,12 +345,12 @@ def run_config(args):
             return ctx.n * k
         work = 0
         for _ in range(k):
-            if ctx.n + emit["per_step"] <= emit["cap"]:
-                xyz, vel = sphcuda.fountain_emit(7, steps_done[0], emit["per_step"], emit["center"], emit["radius"],
-                                                 emit["speed"], emit["sigma"])
-                ctx.append(0, xyz, vel)
+            # the emitter is the step's first phase (generateParticles), generated on the device
             ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             ev0.record(ext)
+            if ctx.n + emit["per_step"] <= emit["cap"]:
+                ctx.emit_fountain(0, 7, steps_done[0], emit["per_step"], emit["center"], emit["radius"],
+                                  emit["speed"], emit["sigma"])
             ctx.step(1)
             ev1.record(ext)
             ev1.synchronize()

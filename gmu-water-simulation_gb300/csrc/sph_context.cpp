@@ -63,6 +63,11 @@ struct sph_ctx {
     std::vector<uint32_t> scene_off_host;
     Tune tune;
     bool tune_pinned = false;  // variants set explicitly: the cache does not override them
+    // front-end handoff (allocated by the first handoff or export)
+    cudaStream_t ho_stream = nullptr;
+    cudaEvent_t ho_ready = nullptr, ho_done = nullptr, ho_export = nullptr;
+    float *ho_xyz = nullptr, *ho_vel = nullptr;
+    bool ho_recorded = false;  // ho_done has been recorded at least once
 };
 
 namespace {
@@ -223,6 +228,9 @@ int allocate(sph_ctx *c)
     return SPH_OK;
 }
 
+// the all-pairs form is O(n^2) per scene: a check for small scenes, not a production path
+constexpr uint32_t kAllPairsMax = 131072;
+
 int create_common(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *scenes, sph_ctx **out)
 {
     if (!out) return fail(nullptr, SPH_ERR_ARG, "out is NULL");
@@ -232,9 +240,21 @@ int create_common(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *
     if (!(p->h > 0) || !(p->dt > 0) || !(p->mass > 0)) return fail(nullptr, SPH_ERR_ARG, "h, dt and mass must be > 0");
     if (p->precision != SPH_PLAIN_F32 && p->precision != SPH_F64 && p->precision != SPH_MIXED)
         return fail(nullptr, SPH_ERR_UNSUPPORTED, "unknown precision form");
+    const bool all_pairs = (p->flags & SPH_FLAG_ALL_PAIRS) != 0;
+    if (all_pairs && p->precision == SPH_MIXED)
+        return fail(nullptr, SPH_ERR_UNSUPPORTED, "the all-pairs form has no mixed-precision variant");
+    for (uint32_t s = 0; all_pairs && s < n_scenes; s++)
+        if (scenes[s].max_particles > kAllPairsMax)
+            return fail(nullptr, SPH_ERR_CAPACITY, "scene " + std::to_string(s) + ": the all-pairs form takes at most " +
+                                                       std::to_string(kAllPairsMax) + " particles per scene");
     sph_ctx *c = new (std::nothrow) sph_ctx();
     if (!c) return fail(nullptr, SPH_ERR_NOMEM, "host allocation failed");
     c->prm = *p;
+    if (all_pairs) {  // both passes over every particle of the scene; no variants to choose
+        c->tune.density_p = Tune::ALL_PAIRS;
+        c->tune.forces_mode = Tune::ALL_PAIRS;
+        c->tune_pinned = true;
+    }
     c->device = p->device;
     uint64_t ctot = 0, ncap = 0;
     for (uint32_t s = 0; s < n_scenes; s++) {
@@ -514,9 +534,15 @@ void sph_destroy(sph_ctx *c)
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->ho_stream) cudaStreamSynchronize(c->ho_stream);
     drop_graph(c);
     for (auto &ev : c->ev)
         if (ev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : {c->ho_ready, c->ho_done, c->ho_export})
+        if (ev) cudaEventDestroy(ev);
+    if (c->ho_stream) cudaStreamDestroy(c->ho_stream);
+    if (c->ho_xyz) cudaFree(c->ho_xyz);
+    if (c->ho_vel) cudaFree(c->ho_vel);
     if (c->pool) cudaFree(c->pool);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -575,33 +601,67 @@ int sph_upload(sph_ctx *c, const float *xyz, const float *vel, const uint32_t *c
     }
 }
 
-int sph_append(sph_ctx *c, uint32_t scene, const float *xyz, const float *vel, uint32_t n)
+namespace {
+
+// checks shared by the two append paths
+int append_check(sph_ctx *c, uint32_t scene, uint32_t n)
 {
-    if (!c) return SPH_ERR_ARG;
     if (scene >= c->sc.size()) return fail(c, SPH_ERR_ARG, "scene index out of range");
     if (n == 0) return SPH_OK;
-    if (!xyz) return fail(c, SPH_ERR_ARG, "xyz is NULL");
     if (c->state != HASHED) return fail(c, SPH_ERR_STATE, "append needs a completed step (or an upload) first");
-    SceneHost &h = c->sc[scene];
+    const SceneHost &h = c->sc[scene];
     if ((uint64_t) h.count + n > h.cap)
         return fail(c, SPH_ERR_CAPACITY, "scene " + std::to_string(scene) + " would exceed its capacity");
-    CK(c, cudaSetDevice(c->device));
-    drop_graph(c);
+    return SPH_OK;
+}
+
+// ingest n particles from the staging arrays as the tail of the scene
+int append_ingest(sph_ctx *c, uint32_t scene, uint32_t n, bool has_vel)
+{
+    SceneHost &h = c->sc[scene];
     if (is_mixed(c)) CK(c, cudaMemsetAsync((char *) c->b.lo_u + 16ull * c->n, 0, 16ull * n, c->stream));
-    CK(c, cudaMemcpyAsync(c->b.st_xyz, xyz, 12ull * n, cudaMemcpyHostToDevice, c->stream));
-    if (vel) CK(c, cudaMemcpyAsync(c->b.st_vel, vel, 12ull * n, cudaMemcpyHostToDevice, c->stream));
     if (is_f64(c))
-        CK(c, Launch<double>::ingest(c->b, c->b.st_xyz, vel ? c->b.st_vel : nullptr, c->n, n, (int32_t) scene, h.count,
-                                     (uint32_t) c->sc.size(), make_consts<double>(c->prm), c->stream));
+        CK(c, Launch<double>::ingest(c->b, c->b.st_xyz, has_vel ? c->b.st_vel : nullptr, c->n, n, (int32_t) scene,
+                                     h.count, (uint32_t) c->sc.size(), make_consts<double>(c->prm), c->stream));
     else
-        CK(c, Launch<float>::ingest(c->b, c->b.st_xyz, vel ? c->b.st_vel : nullptr, c->n, n, (int32_t) scene, h.count,
-                                    (uint32_t) c->sc.size(), make_consts<float>(c->prm), c->stream));
-    // the staging buffers are reused by the next transfer: finish this one first
-    CK(c, cudaStreamSynchronize(c->stream));
+        CK(c, Launch<float>::ingest(c->b, c->b.st_xyz, has_vel ? c->b.st_vel : nullptr, c->n, n, (int32_t) scene,
+                                    h.count, (uint32_t) c->sc.size(), make_consts<float>(c->prm), c->stream));
     h.count += n;
     c->n += n;
     c->appended = true;
     return SPH_OK;
+}
+
+}  // namespace
+
+int sph_append(sph_ctx *c, uint32_t scene, const float *xyz, const float *vel, uint32_t n)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (n != 0 && !xyz) return fail(c, SPH_ERR_ARG, "xyz is NULL");
+    int rc = append_check(c, scene, n);
+    if (rc || n == 0) return rc;
+    CK(c, cudaSetDevice(c->device));
+    drop_graph(c);
+    CK(c, cudaMemcpyAsync(c->b.st_xyz, xyz, 12ull * n, cudaMemcpyHostToDevice, c->stream));
+    if (vel) CK(c, cudaMemcpyAsync(c->b.st_vel, vel, 12ull * n, cudaMemcpyHostToDevice, c->stream));
+    rc = append_ingest(c, scene, n, vel != nullptr);
+    if (rc) return rc;
+    // the caller may reuse or free its host arrays once this returns
+    CK(c, cudaStreamSynchronize(c->stream));
+    return SPH_OK;
+}
+
+int sph_emit_fountain(sph_ctx *c, uint32_t scene, uint64_t seed, uint32_t step, uint32_t n, const float center[3],
+                      float radius, float speed, float sigma)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (!center) return fail(c, SPH_ERR_ARG, "center is NULL");
+    int rc = append_check(c, scene, n);
+    if (rc || n == 0) return rc;
+    CK(c, cudaSetDevice(c->device));
+    drop_graph(c);
+    CK(c, launch_emit_fountain(seed, step, n, center, radius, speed, sigma, c->b.st_xyz, c->b.st_vel, c->stream));
+    return append_ingest(c, scene, n, true);
 }
 
 int sph_set_gravity(sph_ctx *c, int32_t scene, const float g[3])
@@ -707,6 +767,7 @@ int sph_step(sph_ctx *c, int32_t nsteps)
 int sph_set_variant(sph_ctx *c, int32_t density_variant, int32_t forces_variant)
 {
     if (!c) return SPH_ERR_ARG;
+    if (c->prm.flags & SPH_FLAG_ALL_PAIRS) return fail(c, SPH_ERR_STATE, "an all-pairs context has no launch variants");
     if (!valid_density(density_variant) || !valid_forces(forces_variant))
         return fail(c, SPH_ERR_ARG, "unknown launch variant");
     c->tune.density_p = density_variant;
@@ -728,6 +789,7 @@ int sph_autotune(sph_ctx *c, int32_t reps)
 {
     if (!c) return SPH_ERR_ARG;
     if (reps < 1) return fail(c, SPH_ERR_ARG, "reps must be >= 1");
+    if (c->prm.flags & SPH_FLAG_ALL_PAIRS) return fail(c, SPH_ERR_STATE, "an all-pairs context has no launch variants");
     if (c->state != HASHED) return fail(c, SPH_ERR_STATE, "autotune needs a completed step (or an upload)");
     if (c->n == 0) return fail(c, SPH_ERR_STATE, "autotune needs particles");
     CK(c, cudaSetDevice(c->device));
@@ -844,6 +906,111 @@ static int download_impl(sph_ctx *c, void *xyz, void *vel, void *rho, void *p, v
     if (acc) CK(c, cudaMemcpyAsync(acc, sa, 3 * rs * n, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     return SPH_OK;
+}
+
+namespace {
+
+// handoff stream, events and the two float3 buffers of the context's capacity
+int handoff_init(sph_ctx *c)
+{
+    if (c->ho_stream) return SPH_OK;
+    CK(c, cudaStreamCreateWithFlags(&c->ho_stream, cudaStreamNonBlocking));
+    CK(c, cudaEventCreateWithFlags(&c->ho_ready, cudaEventDisableTiming));
+    CK(c, cudaEventCreateWithFlags(&c->ho_done, cudaEventDisableTiming));
+    CK(c, cudaEventCreateWithFlags(&c->ho_export, cudaEventDisableTiming));
+    CK(c, cudaMalloc(&c->ho_xyz, 12 * c->ncap));
+    CK(c, cudaMalloc(&c->ho_vel, 12 * c->ncap));
+    return SPH_OK;
+}
+
+// id-ordered float3 state of every particle into xyz (and vel if not NULL), queued on the
+// context's stream
+int handoff_egress(sph_ctx *c, float *xyz, float *vel)
+{
+    int rc = upload_scene_off(c);
+    if (rc) return rc;
+    const int layout_sorted = (c->state == SORTED || c->state == DENSE) ? 1 : 0;
+    if (is_mixed(c)) {
+        DevBufs hb = c->b;
+        hb.st_xyz = xyz;
+        hb.st_vel = vel ? vel : c->ho_vel;
+        hb.st_acc = nullptr;
+        CK(c, mixed_egress(hb, c->n, 0, 0, layout_sorted, 0, false, c->stream));
+    } else if (is_f64(c)) {
+        CK(c, launch_handoff<double>(c->b, c->n, layout_sorted, xyz, vel, c->stream));
+    } else {
+        CK(c, launch_handoff<float>(c->b, c->n, layout_sorted, xyz, vel, c->stream));
+    }
+    return SPH_OK;
+}
+
+}  // namespace
+
+int sph_handoff_async(sph_ctx *c, float *xyz, float *vel)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (!xyz) return fail(c, SPH_ERR_ARG, "xyz is NULL");
+    if (c->state == EMPTY) return fail(c, SPH_ERR_STATE, "nothing uploaded");
+    try {
+        CK(c, cudaSetDevice(c->device));
+        int rc = handoff_init(c);
+        if (rc) return rc;
+        // the previous copy must have left the handoff buffers before they are rewritten
+        if (c->ho_recorded) CK(c, cudaStreamWaitEvent(c->stream, c->ho_done, 0));
+        rc = handoff_egress(c, c->ho_xyz, c->ho_vel);
+        if (rc) return rc;
+        CK(c, cudaEventRecord(c->ho_ready, c->stream));
+        CK(c, cudaStreamWaitEvent(c->ho_stream, c->ho_ready, 0));
+        const size_t bytes = 12ull * c->n;
+        if (bytes) {
+            CK(c, cudaMemcpyAsync(xyz, c->ho_xyz, bytes, cudaMemcpyDeviceToHost, c->ho_stream));
+            if (vel) CK(c, cudaMemcpyAsync(vel, c->ho_vel, bytes, cudaMemcpyDeviceToHost, c->ho_stream));
+        }
+        CK(c, cudaEventRecord(c->ho_done, c->ho_stream));
+        c->ho_recorded = true;
+        return SPH_OK;
+    } catch (...) {
+        return fail(c, SPH_ERR_NOMEM, "host exception in sph_handoff_async");
+    }
+}
+
+int sph_handoff_ready(sph_ctx *c)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (!c->ho_recorded) return 1;
+    const cudaError_t e = cudaEventQuery(c->ho_done);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    return cuda_fail(c, e, "sph_handoff_ready");
+}
+
+int sph_handoff_wait(sph_ctx *c)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (!c->ho_recorded) return SPH_OK;
+    CK(c, cudaEventSynchronize(c->ho_done));
+    return SPH_OK;
+}
+
+int sph_export_positions(sph_ctx *c, float *dev_xyz, float *dev_vel, void *consumer_stream)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (!dev_xyz) return fail(c, SPH_ERR_ARG, "dev_xyz is NULL");
+    if (c->state == EMPTY) return fail(c, SPH_ERR_STATE, "nothing uploaded");
+    try {
+        CK(c, cudaSetDevice(c->device));
+        int rc = handoff_init(c);
+        if (rc) return rc;
+        rc = handoff_egress(c, dev_xyz, dev_vel);
+        if (rc) return rc;
+        if (consumer_stream) {
+            CK(c, cudaEventRecord(c->ho_export, c->stream));
+            CK(c, cudaStreamWaitEvent((cudaStream_t) consumer_stream, c->ho_export, 0));
+        }
+        return SPH_OK;
+    } catch (...) {
+        return fail(c, SPH_ERR_NOMEM, "host exception in sph_export_positions");
+    }
 }
 
 int sph_download(sph_ctx *c, float *xyz, float *vel, float *rho, float *p, float *acc)

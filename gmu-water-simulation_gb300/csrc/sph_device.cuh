@@ -81,6 +81,8 @@ __device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b)
 __device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float rfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double rfma(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float inv_sqrt(float x) { return rsqrtf(x); }
 __device__ __forceinline__ double inv_sqrt(double x) { return 1.0 / sqrt(x); }
 
@@ -110,24 +112,26 @@ __device__ __forceinline__ SceneDev load_scene(const SceneDev *scenes, uint32_t 
 // (a candidate outside a particle's own 27 cells is farther than h and adds exactly 0).
 // Neighbour test shared by every kernel: r^2 < h^2 as h^2 - r^2 > 0 (the reference's r^2 <= h^2
 // differs only for pairs at exactly r = h, whose density and force terms are 0).
+// The neighbour test h^2 - r^2 > 0 and the poly6 sum, with every rounding explicit (fused
+// multiply-adds in a fixed order) so that each kernel that evaluates them gets the same bits.
 template <class R>
 __device__ __forceinline__ R h2_minus_r2(R dx, R dy, R dz, R h2)
 {
-    R t = h2 - dx * dx;
-    t -= dy * dy;
-    t -= dz * dz;
-    return t;
+    R t = rfma(-dx, dx, h2);
+    t = rfma(-dy, dy, t);
+    return rfma(-dz, dz, t);
 }
+// acc + max(t, 0)^3
 template <class R>
-__device__ __forceinline__ R poly6_from_t(R t)
+__device__ __forceinline__ R poly6_acc(R acc, R t)
 {
     t = t > (R) 0 ? t : (R) 0;
-    return t * t * t;
+    return rfma(rmul(t, t), t, acc);
 }
 template <class R>
-__device__ __forceinline__ R poly6_term(R dx, R dy, R dz, R h2)
+__device__ __forceinline__ R poly6_add(R acc, R dx, R dy, R dz, R h2)
 {
-    return poly6_from_t<R>(h2_minus_r2<R>(dx, dy, dz, h2));
+    return poly6_acc<R>(acc, h2_minus_r2<R>(dx, dy, dz, h2));
 }
 // The two walls of one axis (src/CCollisionGeometry.cpp:117-133 restated per component).
 template <class R>
@@ -243,18 +247,18 @@ __device__ __forceinline__ void pair_terms(const Vec4<R> &pi, const Vec4<R> &vi,
                                            const Vec4<R> &vj, R qj, R invj, const Consts<R> &c, R &fpx, R &fpy,
                                            R &fpz, R &fvx, R &fvy, R &fvz)
 {
-    const R dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-    const R r2 = dx * dx + dy * dy + dz * dz;
+    const R dx = rsub(pi.x, pj.x), dy = rsub(pi.y, pj.y), dz = rsub(pi.z, pj.z);
+    const R r2 = rfma(dz, dz, rfma(dy, dy, rmul(dx, dx)));
     const R rinv = inv_sqrt(r2);
-    const R hr = c.h - r2 * rinv;
-    const R w = (qi + qj) * (c.c_spiky * hr * hr * rinv);  // (p_i/rho_i^2 + p_j/rho_j^2) grad W
-    fpx += w * dx;
-    fpy += w * dy;
-    fpz += w * dz;
-    const R l = c.c_visc * hr * invj;                      // lap W / rho_j
-    fvx += (vj.x - vi.x) * l;
-    fvy += (vj.y - vi.y) * l;
-    fvz += (vj.z - vi.z) * l;
+    const R hr = rfma(-r2, rinv, c.h);
+    const R w = rmul(radd(qi, qj), rmul(rmul(rmul(c.c_spiky, hr), hr), rinv));  // (p_i/rho_i^2 + p_j/rho_j^2) grad W
+    fpx = rfma(w, dx, fpx);
+    fpy = rfma(w, dy, fpy);
+    fpz = rfma(w, dz, fpz);
+    const R l = rmul(rmul(c.c_visc, hr), invj);  // lap W / rho_j
+    fvx = rfma(rsub(vj.x, vi.x), l, fvx);
+    fvy = rfma(rsub(vj.y, vi.y), l, fvy);
+    fvz = rfma(rsub(vj.z, vi.z), l, fvz);
 }
 
 // TwoSum (Knuth): s + e == a + b exactly, s = fl(a + b); explicitly rounded operations.

@@ -113,6 +113,7 @@ struct MixConsts {
 //               of 32/64 entries per thread in shared memory; 3 = driven by the neighbour
 //               masks that the density pass then writes (density_p is ignored)
 struct Tune {
+    static constexpr int ALL_PAIRS = 16;  // both passes over every particle of the scene
     int density_p = 2;
     int forces_mode = 3;
 };
@@ -139,6 +140,14 @@ struct Launch {
 
 // slot assignment of the counting sort alone (the mixed form has its own permute)
 cudaError_t launch_slot(const DevBufs &b, uint32_t n, cudaStream_t st);
+
+// disc emitter on the device (sph_emit.cu): n particles into the float3 staging arrays
+cudaError_t launch_emit_fountain(uint64_t seed, uint32_t step, uint32_t n, const float center[3], float radius,
+                                 float speed, float sigma, float *xyz, float *vel, cudaStream_t st);
+
+// id-ordered float3 positions (and velocities if v) of the first n particles (sph_handoff.cu)
+template <class R>
+cudaError_t launch_handoff(const DevBufs &b, uint32_t n, int layout_sorted, float *xyz, float *v, cudaStream_t st);
 
 // mixed-precision passes (sph_mixed.cu)
 cudaError_t mixed_permute(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, cudaStream_t st);

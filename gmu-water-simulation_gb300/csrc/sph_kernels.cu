@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(256) k_density(const Vec4<R> *__restrict__ pos
 #pragma unroll 4
         for (uint32_t j = jb; j < je; j++) {
             const Vec4<R> pj = ld4(pos + j);
-            acc += poly6_term<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
+            acc = poly6_add<R>(acc, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
         }
     });
     const R rho = rmul(rmul(acc, c.c_poly6), c.mass);
@@ -378,10 +378,9 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
 #pragma unroll 4
                 for (uint32_t j = cb; j < ce; j++) {
                     const Vec4<R> pj = ld4(pos + j);
-                    R t = h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
+                    const R t = h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
                     m = (m >> 1) | (t > (R) 0 ? 0x80000000u : 0u);
-                    t = t > (R) 0 ? t : (R) 0;
-                    acc += t * t * t;
+                    acc = poly6_acc<R>(acc, t);
                 }
                 m >>= 32 - (ce - cb);
                 if (w < MASK_WORDS) masks[(size_t) (r * MASK_WORDS + w) * n + i] = m;
@@ -517,6 +516,75 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask2(
                        cid_out, count);
 }
 
+// All-pairs forms, the reference's brute-force simulator (sph_brute.cl:9-57) restated: every
+// particle of the scene is a candidate, visited in the sorted (cell, id) order. The neighbours
+// accepted by the grid forms are exactly the candidates within h, and the sorted order visits
+// them in the grid forms' candidate order, so both forms sum the same terms in the same order
+// and give the same bits: an independent check of the grid build and the cell windows.
+template <class R>
+__device__ __forceinline__ void scene_range(const SceneDev &sc, const uint32_t *__restrict__ start, uint32_t &jb,
+                                            uint32_t &je)
+{
+    jb = __ldg(start + sc.cell_base);
+    je = __ldg(start + sc.cell_base + (uint32_t) sc.res[0] * (uint32_t) sc.res[1] * (uint32_t) sc.res[2]);
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) k_density_all(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
+                                                     const uint32_t *__restrict__ start,
+                                                     const SceneDev *__restrict__ scenes, uint32_t n, Consts<R> c)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Vec4<R> pi = ld4(pos + i);
+    const SceneDev sc = load_scene(scenes, wbits(pi.w));
+    uint32_t jb, je;
+    scene_range<R>(sc, start, jb, je);
+    R acc = 0;
+    const R h2 = c.h2;
+#pragma unroll 4
+    for (uint32_t j = jb; j < je; j++) {
+        const Vec4<R> pj = ld4(pos + j);
+        acc = poly6_add<R>(acc, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
+    }
+    const R rho = rmul(rmul(acc, c.c_poly6), c.mass);
+    const R p = rmul(c.k, rsub(rho, c.rho0));
+    st4(aux + i, Vec4<R>{rho, p, rdiv(p, rmul(rho, rho)), rdiv((R) 1, rho)});
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) k_forces_all(const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel,
+                                                    const Vec4<R> *__restrict__ aux,
+                                                    const uint32_t *__restrict__ start,
+                                                    const SceneDev *__restrict__ scenes,
+                                                    const ObstacleDev *__restrict__ obstacles, uint32_t n,
+                                                    Consts<R> c, Vec4<R> *__restrict__ pos_out,
+                                                    Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out,
+                                                    uint2 *__restrict__ cid_out, uint32_t *__restrict__ count)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Vec4<R> pi = ld4(pos + i);
+    const Vec4<R> vi = ld4(vel + i);
+    const Vec4<R> ai = ld4(aux + i);
+    const SceneDev sc = load_scene(scenes, wbits(pi.w));
+    uint32_t jb, je;
+    scene_range<R>(sc, start, jb, je);
+    const R h2 = c.h2, qi = ai.z;
+    R fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
+    for (uint32_t j = jb; j < je; j++) {
+        const Vec4<R> pj = ld4(pos + j);
+        if (j != i && h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2) > (R) 0) {
+            const Vec4<R> vj = ld4(vel + j);
+            R qj, invj;
+            ld_qinv(aux + j, qj, invj);
+            pair_terms<R>(pi, vi, qi, pj, vj, qj, invj, c, fpx, fpy, fpz, fvx, fvy, fvz);
+        }
+    }
+    finish_particle<R>(i, pi, vi, ai.x, sc, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
+                       cid_out, count);
+}
+
 // Density, blocked form: each thread owns P consecutive sorted particles. When they share a
 // scene and a (y, z) row of cells (nearly always in sorted order) one candidate scan over the
 // union x-range serves all of them: a candidate outside a particle's own 3 x 3 x 3 block is
@@ -577,7 +645,7 @@ __global__ void __launch_bounds__(256) k_density_blk(const Vec4<R> *__restrict__
                 for (uint32_t j = jb; j < je; j++) {
                     const Vec4<R> pj = ld4(pos + j);
 #pragma unroll
-                    for (int p = 0; p < P; p++) acc[p] += poly6_term<R>(px[p] - pj.x, py[p] - pj.y, pz[p] - pj.z, h2);
+                    for (int p = 0; p < P; p++) acc[p] = poly6_add<R>(acc[p], px[p] - pj.x, py[p] - pj.y, pz[p] - pj.z, h2);
                 }
             }
         }
@@ -595,7 +663,7 @@ __global__ void __launch_bounds__(256) k_density_blk(const Vec4<R> *__restrict__
             for_each_row<R>(sq, start, cx, cy, cz, [&](uint32_t jb, uint32_t je) {
                 for (uint32_t j = jb; j < je; j++) {
                     const Vec4<R> pj = ld4(pos + j);
-                    a += poly6_term<R>(q.x - pj.x, q.y - pj.y, q.z - pj.z, h2);
+                    a = poly6_add<R>(a, q.x - pj.x, q.y - pj.y, q.z - pj.z, h2);
                 }
             });
             acc[p] = a;
@@ -749,6 +817,10 @@ cudaError_t Launch<R>::density(const DevBufs &b, uint32_t n, Consts<R> c, const 
     if (!n) return cudaSuccess;
     const Vec4<R> *pos = (const Vec4<R> *) b.pos_s;
     Vec4<R> *aux = (Vec4<R> *) b.aux;
+    if (t.density_p == Tune::ALL_PAIRS) {
+        k_density_all<R><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c);
+        return cudaGetLastError();
+    }
     if (t.forces_mode >= 3) {  // the mask-driven force passes need the masks
         k_density_mask<R><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c, b.masks);
         return cudaGetLastError();
@@ -770,6 +842,10 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
     const Vec4<R> *pos = (const Vec4<R> *) b.pos_s, *vel = (const Vec4<R> *) b.vel_s, *aux = (const Vec4<R> *) b.aux;
     Vec4<R> *po = (Vec4<R> *) b.pos_u, *vo = (Vec4<R> *) b.vel_u, *ao = record_acc ? (Vec4<R> *) b.acc : nullptr;
     switch (t.forces_mode) {
+    case Tune::ALL_PAIRS:
+        k_forces_all<R><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c, po, vo, ao,
+                                                      b.cid_u, b.count);
+        break;
     case 3:
         k_forces_mask<R, 0><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
                                                           b.masks, po, vo, ao, b.cid_u, b.count);

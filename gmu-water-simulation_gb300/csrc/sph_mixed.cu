@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(256) k_density_mixed(const Vec4<float> *__rest
                     code_delta(gi, __ldg(gpos + j), x, yy, zz);
                     const float t = h2_minus_r2<float>(x, yy, zz, QH2);
                     m = (m >> 1) | (t > 0.0f ? 0x80000000u : 0u);
-                    csum += poly6_from_t<float>(t);
+                    csum = poly6_acc<float>(csum, t);
                 }
                 kahan_add(sum, comp, csum);
                 m >>= 32 - (ce - cb);

@@ -7,6 +7,7 @@
 #include <cstdint>
 
 #include "../../include/sph_cuda.h"
+#include "sph_emit.h"
 
 namespace {
 
@@ -100,24 +101,8 @@ int sph_scene_fountain_emit(uint64_t seed, uint32_t step, uint32_t n, const floa
                             float sigma, float *xyz, float *vel)
 {
     if (!center || !xyz || !vel) return SPH_ERR_ARG;
-    SplitMix64 rng{seed ^ (0xD1B54A32D192ED03ull * ((uint64_t) step + 1))};
-    const double two_pi = 6.283185307179586;
-    for (uint32_t k = 0; k < n; k++) {
-        const double r = (double) radius * std::sqrt(rng.u53());
-        const double t = two_pi * rng.u53();
-        xyz[3 * k + 0] = (float) ((double) center[0] + r * std::cos(t));
-        xyz[3 * k + 1] = center[1];
-        xyz[3 * k + 2] = (float) ((double) center[2] + r * std::sin(t));
-        // Box-Muller normals
-        double g[3];
-        for (int a = 0; a < 3; a++) {
-            const double u1 = 1.0 - rng.u53(), u2 = rng.u53();
-            g[a] = std::sqrt(-2.0 * std::log(u1)) * std::cos(two_pi * u2);
-        }
-        vel[3 * k + 0] = (float) (sigma * g[0]);
-        vel[3 * k + 1] = (float) (speed + sigma * g[1]);
-        vel[3 * k + 2] = (float) (sigma * g[2]);
-    }
+    for (uint32_t k = 0; k < n; k++) sph::emit::particle(seed, step, k, center, radius, speed, sigma, xyz + 3 * (size_t) k,
+                                                         vel + 3 * (size_t) k);
     return SPH_OK;
 }
 

@@ -12,6 +12,7 @@ on a machine without the built library raises.
 import ctypes
 import math
 import os
+import time
 
 import numpy as np
 
@@ -22,15 +23,16 @@ SPH_OK = 0
 SPH_ERR_ARG, SPH_ERR_CUDA, SPH_ERR_CAPACITY, SPH_ERR_STATE, SPH_ERR_NOMEM, SPH_ERR_UNSUPPORTED, SPH_ERR_DEVICE = (
     -1, -2, -3, -4, -5, -6, -7)
 SPH_PLAIN_F32, SPH_F64, SPH_MIXED = 0, 1, 2
-SPH_FLAG_PROFILE, SPH_FLAG_RECORD_ACC = 1, 2
+SPH_FLAG_PROFILE, SPH_FLAG_RECORD_ACC, SPH_FLAG_ALL_PAIRS = 1, 2, 4
 
 # every symbol the header declares
 EXPORTS = (
     "sph_params_default", "sph_create", "sph_batch_create", "sph_destroy", "sph_last_error", "sph_device_name",
     "sph_stream", "sph_set_variant", "sph_get_variant", "sph_autotune", "sph_grid_build_noalloc",
-    "sph_upload", "sph_append", "sph_set_gravity", "sph_step", "sph_pass_grid", "sph_pass_density",
+    "sph_upload", "sph_append", "sph_emit_fountain", "sph_set_gravity", "sph_step", "sph_pass_grid", "sph_pass_density",
     "sph_pass_forces", "sph_pass_times", "sph_get_counts", "sph_num_scenes", "sph_num_particles",
-    "sph_get_resolution", "sph_download", "sph_download_f64", "sph_get_grid", "sph_stats",
+    "sph_get_resolution", "sph_download", "sph_download_f64", "sph_handoff_async", "sph_handoff_ready",
+    "sph_handoff_wait", "sph_export_positions", "sph_get_grid", "sph_stats",
     "sph_scene_reference_dam_break", "sph_scene_lattice", "sph_scene_batch_plan", "sph_scene_fountain_emit",
 )
 
@@ -90,6 +92,7 @@ def load(path=None):
         "sph_grid_build_noalloc": (i32, [vp, u32, fp, f, vp, vp, vp, vp]),
         "sph_upload": (i32, [vp, vp, vp, up]),
         "sph_append": (i32, [vp, u32, vp, vp, u32]),
+        "sph_emit_fountain": (i32, [vp, u32, ctypes.c_uint64, u32, u32, fp, f, f, f]),
         "sph_set_gravity": (i32, [vp, i32, fp]),
         "sph_step": (i32, [vp, i32]),
         "sph_pass_grid": (i32, [vp]), "sph_pass_density": (i32, [vp]), "sph_pass_forces": (i32, [vp]),
@@ -100,6 +103,10 @@ def load(path=None):
         "sph_get_resolution": (i32, [vp, u32, ip]),
         "sph_download": (i32, [vp, vp, vp, vp, vp, vp]),
         "sph_download_f64": (i32, [vp, vp, vp, vp, vp, vp]),
+        "sph_handoff_async": (i32, [vp, vp, vp]),
+        "sph_handoff_ready": (i32, [vp]),
+        "sph_handoff_wait": (i32, [vp]),
+        "sph_export_positions": (i32, [vp, vp, vp, vp]),
         "sph_get_grid": (i32, [vp, up, up, up]),
         "sph_stats": (i32, [vp, u32, dp]),
         "sph_scene_reference_dam_break": (ctypes.c_int64, [f, fp, ctypes.c_uint64]),
@@ -288,6 +295,11 @@ class SphContext:
         vel = None if vel is None else np.ascontiguousarray(vel, np.float32).reshape(-1, 3)
         self._ck(load().sph_append(self.h, scene, _vp(xyz), _vp(vel), xyz.shape[0]))
 
+    def emit_fountain(self, scene, seed, step, n, center, radius, speed, sigma):
+        """Disc emitter on the device (the same particles as fountain_emit)."""
+        c = np.ascontiguousarray(center, np.float32)
+        self._ck(load().sph_emit_fountain(self.h, scene, seed, step, n, _p(c), radius, speed, sigma))
+
     def set_gravity(self, g, scene=-1):
         g = np.ascontiguousarray(g, np.float32)
         self._ck(load().sph_set_gravity(self.h, scene, _p(g)))
@@ -339,6 +351,27 @@ class SphContext:
                                      ctypes.c_void_p(rho_ptr) if rho_ptr else None,
                                      ctypes.c_void_p(p_ptr) if p_ptr else None, None))
 
+    def handoff_async(self, xyz_ptr, vel_ptr=None):
+        """Queue the id-ordered positions (and velocities) into host memory at raw pointers
+        (pinned for an asynchronous copy); see handoff_ready / handoff_wait."""
+        self._ck(load().sph_handoff_async(self.h, ctypes.c_void_p(xyz_ptr),
+                                          ctypes.c_void_p(vel_ptr) if vel_ptr else None))
+
+    def handoff_ready(self):
+        rc = load().sph_handoff_ready(self.h)
+        if rc < 0:
+            self._ck(rc)
+        return rc == 1
+
+    def handoff_wait(self):
+        self._ck(load().sph_handoff_wait(self.h))
+
+    def export_positions(self, dev_xyz_ptr, dev_vel_ptr=None, consumer_stream=None):
+        """Id-ordered float3 positions (and velocities) into device arrays at raw pointers."""
+        self._ck(load().sph_export_positions(self.h, ctypes.c_void_p(dev_xyz_ptr),
+                                             ctypes.c_void_p(dev_vel_ptr) if dev_vel_ptr else None,
+                                             ctypes.c_void_p(consumer_stream) if consumer_stream else None))
+
     def grid(self):
         """(cell of each particle, count of each cell, sorted ids) of the last grid pass."""
         n = self.n
@@ -359,6 +392,53 @@ class SphContext:
 
 # ----------------------------------------------------------------- reference-shaped simulator
 DAM_BREAK, FOUNTAIN = 0, 1  # include/CBaseParticleSimulator.h:21-25
+
+
+class ProfilingEvent:
+    """One step's pass times in ms and the frame rate (sProfilingEvent, include/SProfilingEvent.h:7-31)."""
+
+    __slots__ = ("iteration", "fps", "updateGrid", "updateDensityPressure", "updateForces", "updateCollisions",
+                 "integrate")
+
+    def __init__(self, iteration, fps=0.0, updateGrid=0.0, updateDensityPressure=0.0, updateForces=0.0,
+                 updateCollisions=0.0, integrate=0.0):
+        self.iteration = iteration
+        self.fps = fps
+        self.updateGrid = updateGrid
+        self.updateDensityPressure = updateDensityPressure
+        self.updateForces = updateForces
+        self.updateCollisions = updateCollisions
+        self.integrate = integrate
+
+    def together(self):
+        return self.updateGrid + self.updateDensityPressure + self.updateForces + self.updateCollisions + self.integrate
+
+
+def _qnum(v):
+    """A double as QString::number formats it (format 'g', 6 significant digits)."""
+    return f"{float(v):g}"
+
+
+DETAIL_LABELS = ("Grid", "Density + pressure", "Forces", "Collisions", "Integrate")
+
+
+def export_logs(events, directory, scenario, box_size, simulation_type):
+    """Appends the two profiling logs of MainWindow::exportLogs (src/mainwindow.cpp:310-368):
+    `<scenario>_<box>.csv`, one line `type;together;together;...;` per export, and
+    `<scenario>_<box>_detail.csv`, the type, one `label;v;v;...;` line per pass and two blank
+    lines. Returns the two paths."""
+    os.makedirs(directory, exist_ok=True)
+    stem = os.path.join(directory, f"{scenario}_{_qnum(box_size)}")
+    summary, detail = stem + ".csv", stem + "_detail.csv"
+    with open(summary, "a") as f:
+        f.write(f"{simulation_type};" + "".join(_qnum(e.together()) + ";" for e in events) + "\n")
+    cols = ("updateGrid", "updateDensityPressure", "updateForces", "updateCollisions", "integrate")
+    with open(detail, "a") as f:
+        f.write(f"{simulation_type}\n")
+        for label, col in zip(DETAIL_LABELS, cols):
+            f.write(f"{label};" + "".join(_qnum(getattr(e, col)) + ";" for e in events) + "\n")
+        f.write("\n\n")
+    return summary, detail
 
 
 class CCUDAParticleSimulator:
@@ -386,6 +466,11 @@ class CCUDAParticleSimulator:
         self._gravity = np.array([0.0, -9.80665, 0.0], np.float32)
         self._times = np.zeros(5)
         self._pending = None
+        # profiling log (include/CBaseParticleSimulator.h:54-55): one event every 10 steps
+        self.events = []
+        self.eventLoggerStride = 10
+        self.iterationSincePaused = 0
+        self._t0 = time.perf_counter()
 
     def getSelectedDevice(self):
         return self.ctx.device_name if self.ctx else ""
@@ -461,7 +546,10 @@ class CCUDAParticleSimulator:
             self.integrate()
             if self.flags & SPH_FLAG_PROFILE:
                 self._times = self.ctx.pass_times()
+                if self.totalIteration % self.eventLoggerStride == 0:
+                    self.events.append(ProfilingEvent(self.totalIteration, self.getFps(), *self._times))
             self.totalIteration += 1
+            self.iterationSincePaused += 1
         except SphError as exc:
             self.running = False
             if self.errorOccured:
@@ -473,8 +561,20 @@ class CCUDAParticleSimulator:
         """(grid, density, forces, collisions, integrate) ms of the last step."""
         return self._times
 
+    def getFps(self):
+        """Steps per second since the simulation was last started (CBaseParticleSimulator::getFps)."""
+        el = time.perf_counter() - self._t0
+        return self.iterationSincePaused / el if el > 0 else 0.0
+
+    def exportLogs(self, directory, simulationType="GPU CUDA", scenarioName=None):
+        """The profiling logs of MainWindow::exportLogs for this simulator's events."""
+        name = scenarioName or ("Dam break" if self.m_scenario == DAM_BREAK else "Fountain")
+        return export_logs(self.events, directory, name, float(self.m_boxSize), simulationType)
+
     def start(self):
         self.running = True
+        self.iterationSincePaused = 0
+        self._t0 = time.perf_counter()
 
     def stop(self):
         self.running = False

@@ -12,7 +12,9 @@
 #ifndef CCUDAPARTICLESIMULATOR_HPP
 #define CCUDAPARTICLESIMULATOR_HPP
 
+#include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <functional>
 #include <stdexcept>
 #include <string>
@@ -21,6 +23,14 @@
 #include "sph_cuda.h"
 
 enum SimulationScenario { DAM_BREAK = 0, FOUNTAIN };  // include/CBaseParticleSimulator.h:21-25
+
+// One step's pass times in ms and the frame rate (include/SProfilingEvent.h:7-31).
+struct sProfilingEvent {
+    unsigned long iteration;
+    double fps = 0, updateGrid = 0, updateDensityPressure = 0, updateForces = 0, updateCollisions = 0, integrate = 0;
+    explicit sProfilingEvent(unsigned long it) : iteration(it) {}
+    double together() const { return updateGrid + updateDensityPressure + updateForces + updateCollisions + integrate; }
+};
 
 class CCUDAParticleSimulator
 {
@@ -91,14 +101,30 @@ public:
             m_last[2] = updateForces();
             m_last[3] = updateCollisions();
             m_last[4] = integrate();
+            if (m_profiling && m_totalIteration % eventLoggerStride == 0) {  // src/CBaseParticleSimulator.cpp:138-142
+                sProfilingEvent e(m_totalIteration);
+                e.fps = getFps();
+                e.updateGrid = m_last[0];
+                e.updateDensityPressure = m_last[1];
+                e.updateForces = m_last[2];
+                e.updateCollisions = m_last[3];
+                e.integrate = m_last[4];
+                events.push_back(e);
+            }
             ++m_totalIteration;
+            ++m_iterationSincePaused;
         } catch (const SphException &e) {
             if (errorOccured) errorOccured(e.what());
             stop();
         }
     }
 
-    void start() { m_running = true; }
+    void start()
+    {
+        m_running = true;
+        m_iterationSincePaused = 0;
+        m_t0 = std::chrono::steady_clock::now();
+    }
     void stop() { m_running = false; }
     bool isRunning() const { return m_running; }
 
@@ -107,6 +133,51 @@ public:
     unsigned long getTotalIteration() const { return m_totalIteration; }
     const double *lastPassTimes() const { return m_last; }  // grid, density, forces, collisions, integrate
     sph_ctx *context() { return m_ctx; }
+
+    // profiling log (include/CBaseParticleSimulator.h:54-55)
+    std::vector<sProfilingEvent> events;
+    int eventLoggerStride = 10;
+
+    // steps per second since the simulation was last started (CBaseParticleSimulator::getFps)
+    double getFps() const
+    {
+        const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - m_t0).count();
+        return el > 0 ? m_iterationSincePaused / el : 0.0;
+    }
+
+    // Appends the two profiling logs of MainWindow::exportLogs (src/mainwindow.cpp:310-368) to
+    // <dir>/<scenario>_<box>.csv (one "type;together;...;" line) and <dir>/<scenario>_<box>_detail.csv
+    // (the type, one "label;v;...;" line per pass, two blank lines). Numbers as QString::number
+    // prints them (%g). Returns false if a file cannot be opened; the directory must exist.
+    bool exportLogs(const std::string &dir, const std::string &simulationType, const std::string &scenarioName) const
+    {
+        const std::string stem = dir + "/" + scenarioName + "_" + num(m_boxSize);
+        FILE *f = std::fopen((stem + ".csv").c_str(), "a");
+        FILE *d = std::fopen((stem + "_detail.csv").c_str(), "a");
+        if (!f || !d) {
+            if (f) std::fclose(f);
+            if (d) std::fclose(d);
+            return false;
+        }
+        std::string line = simulationType + ";";
+        std::string rows[5];
+        for (const auto &e : events) {
+            line += num(e.together()) + ";";
+            rows[0] += num(e.updateGrid) + ";";
+            rows[1] += num(e.updateDensityPressure) + ";";
+            rows[2] += num(e.updateForces) + ";";
+            rows[3] += num(e.updateCollisions) + ";";
+            rows[4] += num(e.integrate) + ";";
+        }
+        std::fputs((line + "\n").c_str(), f);
+        static const char *labels[5] = {"Grid", "Density + pressure", "Forces", "Collisions", "Integrate"};
+        std::string det = simulationType + "\n";
+        for (int k = 0; k < 5; k++) det += std::string(labels[k]) + ";" + rows[k] + "\n";
+        std::fputs((det + "\n\n").c_str(), d);
+        std::fclose(f);
+        std::fclose(d);
+        return true;
+    }
 
     // id-ordered state, as CGPUBaseParticleSimulator::integrate reads it back
     void readState(std::vector<float> &xyz, std::vector<float> &vel, std::vector<float> &rho)
@@ -141,6 +212,13 @@ public:
     double integrate() { return 0.0; }         // fused into updateForces
 
 private:
+    static std::string num(double v)
+    {
+        char b[64];
+        std::snprintf(b, sizeof b, "%g", v);
+        return b;
+    }
+
     void check(int rc, bool creating = false)
     {
         if (rc != SPH_OK) throw SphException(rc, sph_last_error(creating ? nullptr : m_ctx));
@@ -173,6 +251,8 @@ private:
     unsigned long m_particlesCount = 0, m_maxParticlesCount = 0, m_totalIteration = 0;
     bool m_running = false;
     double m_last[5] = {0, 0, 0, 0, 0};
+    unsigned long m_iterationSincePaused = 0;
+    std::chrono::steady_clock::time_point m_t0 = std::chrono::steady_clock::now();
 };
 
 #endif  // CCUDAPARTICLESIMULATOR_HPP

@@ -45,6 +45,12 @@ extern "C" {
 /* sph_params.flags */
 #define SPH_FLAG_PROFILE 1u    /* record per-pass CUDA-event times (sph_pass_times) */
 #define SPH_FLAG_RECORD_ACC 2u /* keep each step's accelerations for sph_download */
+/* Density and force passes over every particle of a scene instead of the 27 grid cells: the
+ * reference's brute-force simulator (CGPUBruteParticleSimulator, sph_brute.cl:9-57). Visited
+ * in the sorted order, the accepted neighbours and their order are the grid form's, so the
+ * result is bit-identical to the grid form: an independent check of the grid, for scenes of
+ * at most 131,072 particles (SPH_ERR_CAPACITY beyond). Not with SPH_MIXED; no launch variants. */
+#define SPH_FLAG_ALL_PAIRS 4u
 
 typedef struct sph_ctx sph_ctx;
 
@@ -117,6 +123,16 @@ int sph_upload(sph_ctx *ctx, const float *xyz, const float *vel, const uint32_t 
  * generateParticles, src/CBaseParticleSimulator.cpp:187-210). */
 int sph_append(sph_ctx *ctx, uint32_t scene, const float *xyz, const float *vel, uint32_t n);
 
+/* The disc emitter on the device: appends n particles to a scene like sph_append, generated
+ * on the GPU (no host arrays, no host-to-device copy, no host synchronisation). Particle k of
+ * emission step `step` lies on the disc of `radius` around center in the plane y = center[1],
+ * with velocity (0, speed, 0) + sigma * N(0, I). The particles are bit-identical to
+ * sph_scene_fountain_emit's with the same arguments. Generalises the reference's FOUNTAIN
+ * source (src/CBaseParticleSimulator.cpp:187-210, 7 particles per step). Same state and
+ * capacity errors as sph_append. */
+int sph_emit_fountain(sph_ctx *ctx, uint32_t scene, uint64_t seed, uint32_t step, uint32_t n, const float center[3],
+                      float radius, float speed, float sigma);
+
 /* CGPUBaseParticleSimulator::setGravityVector (src/CGPUBaseParticleSimulator.cpp:11-15).
  * scene < 0 sets every scene. */
 int sph_set_gravity(sph_ctx *ctx, int32_t scene, const float g[3]);
@@ -175,6 +191,27 @@ int sph_download(sph_ctx *ctx, float *xyz, float *vel, float *rho, float *p, flo
 /* Same in double, for SPH_F64 contexts. */
 int sph_download_f64(sph_ctx *ctx, double *xyz, double *vel, double *rho, double *p, double *acc);
 
+/* Front-end handoff without a synchronising download. The reference reads the whole particle
+ * buffer back and updates every CParticle after each step (CGPUBaseParticleSimulator::integrate,
+ * src/CGPUBaseParticleSimulator.cpp:76-97). sph_handoff_async queues, after the work already
+ * queued on the context's stream, the id-ordered float3 positions (and velocities if vel is
+ * not NULL) of every particle, and copies them to xyz/vel on a second stream, so that the
+ * steps queued next overlap the copy. Use pinned host memory (cudaHostAlloc) for an
+ * asynchronous copy. The arrays must stay valid until sph_handoff_ready returns 1 or
+ * sph_handoff_wait returns. A handoff waits for the previous handoff's copy before it
+ * rewrites the handoff buffers (3 floats x 2 x capacity, allocated by the first call).
+ * FP64 and mixed contexts deliver their state rounded to float. */
+int sph_handoff_async(sph_ctx *ctx, float *xyz, float *vel);
+/* 1 once the last handoff's copy has landed (or none was queued), 0 while it is in flight. */
+int sph_handoff_ready(sph_ctx *ctx);
+/* Blocks until the last handoff's copy has landed. */
+int sph_handoff_wait(sph_ctx *ctx);
+/* The same id-ordered float3 positions (and velocities if dev_vel is not NULL) into device
+ * arrays of the caller (3 floats per particle each), e.g. a renderer's vertex buffer mapped
+ * into CUDA. Queued on the context's stream; consumer_stream (a cudaStream_t, or NULL) is made
+ * to wait for it. */
+int sph_export_positions(sph_ctx *ctx, float *dev_xyz, float *dev_vel, void *consumer_stream);
+
 /* The grid of the last grid pass: the cell of every particle (scene-major, id order,
  * cell index local to its scene: x + y*X + z*X*Y), the count of every cell (scene-major),
  * and the ids of each scene's particles in sorted order, ascending (cell, id). Any
@@ -222,7 +259,8 @@ int sph_scene_batch_plan(uint32_t n_scenes, uint64_t seed, uint32_t nmin, uint32
                          uint32_t *dims, float *boxes);
 
 /* Disc emitter: n particles on a disc of the given radius in the y = center[1] plane,
- * velocity (0, speed, 0) plus N(0, sigma^2) per component; seeded by (seed, step). */
+ * velocity (0, speed, 0) plus N(0, sigma^2) per component. Particle k draws from its own
+ * stream seeded by (seed, step, k); sph_emit_fountain generates the same bits on the device. */
 int sph_scene_fountain_emit(uint64_t seed, uint32_t step, uint32_t n, const float center[3], float radius, float speed,
                             float sigma, float *xyz, float *vel);
 

@@ -17,8 +17,9 @@ static int failures = 0;
         }                                                                      \
     } while (0)
 
-int main()
+int main(int argc, char **argv)
 {
+    const std::string logdir = argc > 1 ? argv[1] : ".";
     {
         CCUDAParticleSimulator sim(0.4f, DAM_BREAK);
         sim.setupScene();
@@ -41,6 +42,21 @@ int main()
         sim.setGravityVector(g);
         sim.step();
         CHECK(sim.getTotalIteration() == 4);
+        // the profiling log: events at iterations 0, 10, 20 and the reference's two CSV files
+        for (int k = 0; k < 17; k++) sim.step();
+        CHECK(sim.events.size() == 3 && sim.events[2].iteration == 20);
+        CHECK(sim.events[1].updateForces > 0 && sim.events[2].fps > 0);
+        CHECK(sim.exportLogs(logdir, "GPU CUDA", "Dam break"));
+        FILE *f = std::fopen((logdir + "/Dam break_0.4.csv").c_str(), "r");
+        CHECK(f != nullptr);
+        if (f) {
+            char line[512] = {0};
+            CHECK(std::fgets(line, sizeof line, f) != nullptr);
+            int semis = 0;
+            for (char *q = line; *q; q++) semis += *q == ';';
+            CHECK(std::string(line).rfind("GPU CUDA;", 0) == 0 && semis == 4);
+            std::fclose(f);
+        }
         // an out-of-order pass makes the next step fail: the simulator stops and signals
         std::string msg;
         sim.errorOccured = [&](const char *m) { msg = m; };

@@ -69,6 +69,11 @@ def test_argument_errors_without_gpu(sphlib):
     box = (ctypes.c_float * 3)(1, 1, 1)
     rc = sphlib.load().sph_create(ctypes.byref(p), box, 10, ctypes.byref(hh))
     assert rc == sphlib.SPH_ERR_ARG and b"struct_size" in sphlib.load().sph_last_error(None)
+    # the all-pairs form: no mixed-precision variant, small scenes only
+    rc, h, msg = _create(sphlib, precision=sphlib.SPH_MIXED, flags=sphlib.SPH_FLAG_ALL_PAIRS)
+    assert rc == sphlib.SPH_ERR_UNSUPPORTED and "all-pairs" in msg
+    rc, h, msg = _create(sphlib, cap=131073, flags=sphlib.SPH_FLAG_ALL_PAIRS)
+    assert rc == sphlib.SPH_ERR_CAPACITY and "131072" in msg
     # NULL context pointers are rejected, never dereferenced
     L = sphlib.load()
     assert L.sph_step(None, 1) == sphlib.SPH_ERR_ARG

@@ -25,5 +25,5 @@ def test_cpp_mirror_compiles(sphlib, tmp_path):
 @pytest.mark.gpu
 def test_cpp_mirror_runs(sphlib, tmp_path):
     exe = build_binary(sphlib, tmp_path)
-    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    r = subprocess.run([exe, str(tmp_path)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr

@@ -255,7 +255,127 @@ def test_append_between_steps(sphlib, oracle_mod):
     ctx.close()
 
 
-def test_reference_shaped_simulator(sphlib, oracle_mod):
+@pytest.mark.parametrize("prec", ["plain", "f64"])
+def test_all_pairs_equals_grid(sphlib, prec):
+    """The all-pairs form (the reference's brute-force simulator) and the grid form give the
+    same bits over several steps: one scene with obstacles, then a batch of three scenes."""
+    P = {"plain": sphlib.SPH_PLAIN_F32, "f64": sphlib.SPH_F64}[prec]
+    box = (1.0, 1.0, 0.5)
+    pos = sphlib.dam_break_scene((20, 20, 20), box, seed=0)
+    obstacles = [np.array([0.1, -0.5, -0.1, 0.3, -0.3, 0.1], np.float32)]
+    runs = []
+    for flags in (0, sphlib.SPH_FLAG_ALL_PAIRS):
+        ctx = sphlib.SphContext(box, pos.shape[0], precision=P, flags=flags | sphlib.SPH_FLAG_RECORD_ACC,
+                                gravity=G981, obstacles=obstacles)
+        ctx.upload(pos)
+        ctx.step(12)
+        runs.append(ctx.download(acc=True))
+        if flags:
+            with pytest.raises(sphlib.SphError) as e:
+                ctx.set_variant(0, 3)
+            assert e.value.code == sphlib.SPH_ERR_STATE
+        ctx.close()
+    for k in runs[0]:
+        assert np.array_equal(runs[0][k], runs[1][k]), k
+    dims, boxes = sphlib.batch_plan(3, seed=5, nmin=500, nmax=4000)
+    parts = [sphlib.dam_break_scene(tuple(int(x) for x in d), tuple(float(x) for x in b), seed=s)
+             for s, (d, b) in enumerate(zip(dims, boxes))]
+    counts = [q.shape[0] for q in parts]
+    runs = []
+    for flags in (0, sphlib.SPH_FLAG_ALL_PAIRS):
+        ctx = sphlib.SphContext(boxes, counts, precision=P, flags=flags, gravity=G981)
+        ctx.upload(np.concatenate(parts), None, counts)
+        ctx.step(7)
+        runs.append(ctx.download())
+        ctx.close()
+    for k in runs[0]:
+        assert np.array_equal(runs[0][k], runs[1][k]), k
+
+
+@pytest.mark.parametrize("prec", ["plain", "f64", "mixed"])
+def test_handoff_and_export(sphlib, prec):
+    """The asynchronous handoff delivers the state of the moment it was queued while later
+    steps run, leaves the run unchanged, and the device export gives the same float3 arrays."""
+    import torch
+
+    P = {"plain": sphlib.SPH_PLAIN_F32, "f64": sphlib.SPH_F64, "mixed": sphlib.SPH_MIXED}[prec]
+    pos = c0_scene(sphlib, dims=(16, 16, 16))
+    n = pos.shape[0]
+
+    def now(ctx):
+        if prec == "f64":
+            import ctypes
+            L = sphlib.load()
+            x = np.zeros((n, 3)); v = np.zeros((n, 3))
+            L.sph_download_f64(ctx.h, ctypes.c_void_p(x.ctypes.data), ctypes.c_void_p(v.ctypes.data), None, None, None)
+            return x.astype(np.float32), v.astype(np.float32)
+        d = ctx.download()
+        return d["pos"], d["vel"]
+
+    a = sphlib.SphContext(C0_BOX, n, precision=P, gravity=G981)
+    a.upload(pos)
+    a.step(5)
+    ref_x, ref_v = now(a)
+    a.step(9)
+    fin_x, fin_v = now(a)
+    b = sphlib.SphContext(C0_BOX, n, precision=P, gravity=G981)
+    b.upload(pos)
+    b.step(5)
+    hx = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+    hv = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+    b.handoff_async(hx.data_ptr(), hv.data_ptr())
+    b.step(9)  # queued behind the handoff's egress, overlapping its copy
+    b.handoff_wait()
+    assert b.handoff_ready()
+    assert np.array_equal(hx.numpy(), ref_x) and np.array_equal(hv.numpy(), ref_v)
+    got_x, got_v = now(b)
+    assert np.array_equal(got_x, fin_x) and np.array_equal(got_v, fin_v)
+    # a second handoff reuses the buffers after the first copy
+    b.handoff_async(hx.data_ptr(), None)
+    b.handoff_wait()
+    assert np.array_equal(hx.numpy(), fin_x)
+    dx = torch.full((n, 3), float("nan"), dtype=torch.float32, device="cuda")
+    dv = torch.full((n, 3), float("nan"), dtype=torch.float32, device="cuda")
+    side = torch.cuda.Stream()
+    b.export_positions(dx.data_ptr(), dv.data_ptr(), side.cuda_stream)
+    with torch.cuda.stream(side):
+        sx, sv = dx.cpu(), dv.cpu()
+    assert np.array_equal(sx.numpy(), fin_x) and np.array_equal(sv.numpy(), fin_v)
+    a.close()
+    b.close()
+
+
+def test_device_emitter_equals_host_emitter(sphlib):
+    """sph_emit_fountain generates on the device the same bits as the host generator, and a run
+    fed by it equals a run fed by sph_append of the host-generated particles."""
+    box = (0.6, 0.6, 0.6)
+    args = dict(center=(0.0, -0.29, 0.0), radius=0.05, speed=1.0, sigma=0.05)
+    a = sphlib.SphContext(box, 5000)
+    b = sphlib.SphContext(box, 5000)
+    for c in (a, b):
+        c.upload(np.zeros((0, 3), np.float32))
+    for k in range(6):
+        xyz, vel = sphlib.fountain_emit(seed=4, step=k, n=333, **args)
+        a.append(0, xyz, vel)
+        b.emit_fountain(0, 4, k, 333, args["center"], args["radius"], args["speed"], args["sigma"])
+        if k == 0:
+            da, db = a.download(), b.download()
+            assert np.array_equal(da["pos"], db["pos"]) and np.array_equal(da["vel"], db["vel"])
+            assert np.array_equal(db["pos"], xyz) and np.array_equal(db["vel"], vel)
+        a.step(1)
+        b.step(1)
+    da, db = a.download(), b.download()
+    assert a.n == b.n == 6 * 333
+    for k in ("pos", "vel", "rho"):
+        assert np.array_equal(da[k], db[k]), k
+    with pytest.raises(sphlib.SphError) as e:
+        b.emit_fountain(0, 4, 7, 3003, args["center"], args["radius"], args["speed"], args["sigma"])
+    assert e.value.code == sphlib.SPH_ERR_CAPACITY
+    a.close()
+    b.close()
+
+
+def test_reference_shaped_simulator(sphlib, oracle_mod, tmp_path):
     """The CBaseParticleSimulator mirror: setupScene + step on the 0.4 m dam break matches the
     oracle, and the FOUNTAIN scenario emits 7 particles per step."""
     sim = sphlib.CCUDAParticleSimulator(0.4, sphlib.DAM_BREAK)
@@ -274,6 +394,16 @@ def test_reference_shaped_simulator(sphlib, oracle_mod):
         f.step()
     assert f.getParticlesCount() == 35 and f.ctx.n == 35
     assert f.getMaxParticlesCount() == 1620
+    # the profiling log: an event every 10 steps with the passes' event times, exported as the
+    # reference's two CSV files
+    for _ in range(20):
+        sim.step()
+    assert [e.iteration for e in sim.events] == [0, 10, 20]
+    assert all(e.updateGrid > 0 and e.updateDensityPressure > 0 and e.updateForces > 0 for e in sim.events)
+    assert sim.events[-1].fps > 0
+    s, d = sim.exportLogs(str(tmp_path))
+    assert os.path.basename(s) == "Dam break_0.4.csv" and open(s).read().count(";") == 4
+    assert open(d).read().splitlines()[1].startswith("Grid;")
 
 
 def test_errors_are_status_codes(sphlib):

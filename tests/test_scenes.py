@@ -95,3 +95,27 @@ def test_fountain_emitter(sphlib):
     assert abs(vel[:, 1].mean() - 5.0) < 0.03 and abs(vel[:, 0].std() - 0.2) < 0.02
     x3, _ = sphlib.fountain_emit(seed=2, step=6, n=2000, center=(0.0, -0.99, 0.0), radius=0.05, speed=5.0, sigma=0.2)
     assert not np.array_equal(xyz, x3)
+
+
+def test_fountain_emitter_distribution(sphlib):
+    """The emitter's normals (Marsaglia's polar method with the generator's own logarithm) and
+    its disc sampling have the stated distribution."""
+    n = 200000
+    xyz, vel = sphlib.fountain_emit(seed=9, step=0, n=n, center=(0.0, 0.0, 0.0), radius=1.0, speed=0.0, sigma=1.0)
+    g = vel.astype(np.float64)
+    assert np.all(np.abs(g.mean(axis=0)) < 0.01)
+    assert np.all(np.abs(g.std(axis=0) - 1.0) < 0.01)
+    # fourth moment of a normal is 3 (standard error 0.022 at this n); the tails are present
+    assert np.all(np.abs((g ** 4).mean(axis=0) - 3.0) < 0.1)
+    assert np.all(np.abs(g).max(axis=0) > 4.0)
+    stats = pytest.importorskip("scipy.stats")
+    for a in range(3):
+        assert stats.kstest(g[:, a], "norm").pvalue > 1e-4
+    r2 = xyz[:, 0].astype(np.float64) ** 2 + xyz[:, 2].astype(np.float64) ** 2
+    assert r2.max() <= 1.0 + 1e-6
+    # uniform on the disc: P(r^2 < t) = t
+    for t in (0.1, 0.25, 0.5, 0.9):
+        assert abs(np.mean(r2 < t) - t) < 0.005
+    # particles of one step are independent of how many are drawn
+    x2, v2 = sphlib.fountain_emit(seed=9, step=0, n=100, center=(0.0, 0.0, 0.0), radius=1.0, speed=0.0, sigma=1.0)
+    assert np.array_equal(x2, xyz[:100]) and np.array_equal(v2, vel[:100])
