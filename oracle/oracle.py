@@ -2,9 +2,12 @@
 
 The oracle is a CPU restatement of the reference's serial SPH step
 (src/CCPUParticleSimulator.cpp:9-229); see sph_oracle.c for the line-by-line
-citations. PARITY UNPINNED: the reference cannot be built here (Qt5/Qt3D absent)
-and ships no golden vectors; the restatement is pinned to analytic known answers
-and to the reference's scene-count assert only.
+citations. The reference's CPU simulator cannot be built here (Qt5/Qt3D absent) and ships
+no golden vectors. Its own OpenCL grid kernels (resources/kernels/sph_grid.cl,
+sph_common.cl) compile for the CPU through oracle/ref_cl where the reference tree is present
+(build_ref): they pin this restatement's density, pressure and forces and generate the golden
+vectors under tests/golden/. The walls, integration and cell hash are pinned to analytic
+known answers and to the reference's scene-count assert.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module.
 """
@@ -35,6 +38,69 @@ def build(force=False):
         subprocess.check_call([os.environ.get("CC", "gcc"), *CFLAGS, "-o", tmp, src, "-lm"])
         os.replace(tmp, LIB_PATH)
     return LIB_PATH
+
+
+# The reference's own OpenCL kernels compiled for the CPU (oracle/ref_cl): built only where the
+# reference tree is present, into oracle/_ref/ (not committed, not usable on another machine).
+REF_KERNELS = os.environ.get("SPH_REF_KERNELS", "/root/reference/resources/kernels")
+REF_DIR = os.path.join(HERE, "_ref")
+REF_LIB = os.path.join(REF_DIR, "librefcl.so")
+_ref = None
+
+
+def build_ref(force=False):
+    """Compile oracle/ref_cl/ref_cl.cpp, which includes sph_common.cl and sph_grid.cl from the
+    reference tree where they lie, into oracle/_ref/librefcl.so. Returns the path, or None when
+    the reference tree is absent."""
+    srcs = [os.path.join(REF_KERNELS, f) for f in ("sph_common.cl", "sph_grid.cl")]
+    if not all(os.path.exists(f) for f in srcs):
+        return None
+    here = os.path.join(HERE, "ref_cl")
+    deps = srcs + [os.path.join(here, f) for f in ("ref_cl.cpp", "cl_shim.h")]
+    if force or not os.path.exists(REF_LIB) or os.path.getmtime(REF_LIB) < max(os.path.getmtime(f) for f in deps):
+        os.makedirs(REF_DIR, exist_ok=True)
+        tmp = REF_LIB + ".tmp"
+        subprocess.check_call([os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC", "-shared",
+                               "-ffp-contract=off", "-Wno-unknown-pragmas", "-Wno-unused-value",
+                               "-Wno-unused-variable", "-I", here, "-I", REF_KERNELS,
+                               os.path.join(here, "ref_cl.cpp"), "-o", tmp])
+        os.replace(tmp, REF_LIB)
+    return REF_LIB
+
+
+def ref_lib():
+    """The compiled reference kernels, or None where they were not built."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_LIB):
+            return None
+        try:
+            L = ctypes.CDLL(REF_LIB)
+        except OSError:  # built for another machine
+            return None
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.refcl_density_forces.argtypes = [ctypes.c_int, fp, fp, fp, fp, fp, fp, fp]
+        L.refcl_density_forces.restype = ctypes.c_int
+        _ref = L
+    return _ref
+
+
+def ref_density_forces(pos, vel, box, gravity):
+    """The reference's density_pressure_step and forces_step (sph_grid.cl) for one state:
+    (rho, p, acc before the walls), in input order."""
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("reference kernels not built (oracle.build_ref)")
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    vel = np.ascontiguousarray(vel, np.float32).reshape(-1, 3)
+    n = pos.shape[0]
+    b = np.ascontiguousarray(np.broadcast_to(np.asarray(box, np.float32), (3,)))
+    g = np.ascontiguousarray(gravity, np.float32)
+    rho, p, acc = np.zeros(n, np.float32), np.zeros(n, np.float32), np.zeros((n, 3), np.float32)
+    rc = L.refcl_density_forces(n, _f(pos), _f(vel), _f(b), _f(g), _f(rho), _f(p), _f(acc))
+    if rc:
+        raise ValueError("refcl_density_forces failed")
+    return rho, p, acc
 
 
 def lib():

@@ -11,11 +11,14 @@
  * A CPU restatement of the all-pairs kernels (resources/kernels/sph_brute.cl:9-57)
  * serves as an independent second check.
  *
- * PARITY UNPINNED: the reference cannot be built here (its CPU path needs Qt5Gui
- * QVector3D and Qt3D, which are absent) and it ships no tests, fixtures or golden
- * vectors. This restatement is pinned only to analytic known answers (self
- * density, hand-placed particle pairs evaluated independently in high precision)
- * and to the reference's own scene-count assert (src/CBaseParticleSimulator.cpp:56).
+ * The reference's CPU path cannot be built here (it needs Qt5Gui QVector3D and
+ * Qt3D, which are absent) and it ships no tests, fixtures or golden vectors. The
+ * density, pressure and forces of this restatement are pinned to the reference's
+ * own OpenCL grid kernels compiled for the CPU (oracle/ref_cl, golden vectors in
+ * tests/golden/ref_cl_cases.npz); the walls, integration and cell hash to analytic
+ * known answers (self density, hand-placed particle pairs evaluated independently
+ * in high precision) and to the reference's own scene-count assert
+ * (src/CBaseParticleSimulator.cpp:56).
  *
  * Arithmetic is restated operation by operation. Qt5's QVector3D stores floats;
  * its +, -, * float, / float, dotProduct and lengthSquared are float operations

@@ -255,6 +255,29 @@ def test_append_between_steps(sphlib, oracle_mod):
     ctx.close()
 
 
+def test_gpu_matches_reference_kernels(sphlib, oracle_mod):
+    """One plain FP32 step on the golden states against the reference's own OpenCL kernels
+    (density, pressure; acceleration away from the walls), within the 1e-5 parity band."""
+    from test_oracle import interior, ref_cl_cases
+
+    for c in ref_cl_cases():
+        box = tuple(float(b) for b in c["box"])
+        ctx = sphlib.SphContext(box, c["pos"].shape[0], flags=sphlib.SPH_FLAG_RECORD_ACC, gravity=c["gravity"])
+        ctx.upload(c["pos"], c["vel"])
+        ctx.step(1)
+        got = ctx.download(acc=True)
+        ctx.close()
+        o = oracle_mod.Oracle(box, oracle_mod.REF, threads=4, gravity=c["gravity"])
+        o.add(c["pos"], c["vel"])
+        o.step(1)
+        s = o.state()  # the per-particle force scale A
+        inside = interior(c["pos"], box)
+        errs = rel_errors({"rho": got["rho"], "p": got["p"]}, {"rho": c["rho"], "p": c["p"]})
+        errs.update(rel_errors({"acc": got["acc"][inside]},
+                               {"rho": c["rho"][inside], "acc": c["acc"][inside], "ascale": s["ascale"][inside]}))
+        assert_within(errs, c["name"])
+
+
 @pytest.mark.parametrize("prec", ["plain", "f64"])
 def test_all_pairs_equals_grid(sphlib, prec):
     """The all-pairs form (the reference's brute-force simulator) and the grid form give the

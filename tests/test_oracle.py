@@ -197,3 +197,53 @@ def test_ref_order_is_history_dependent(oracle_mod):
     cell, counts, order = o.grid()
     assert counts.sum() == pos.shape[0]
     assert np.all(np.diff(cell[order]) >= 0)
+
+
+# ---------------------------------------------------------------- the reference's own kernels
+REF_CL = os.path.join(os.path.dirname(__file__), "golden", "ref_cl_cases.npz")
+
+
+def ref_cl_cases():
+    """Golden outputs of the reference's OpenCL density_pressure_step and forces_step
+    (resources/kernels/sph_grid.cl) compiled for the CPU (tests/golden/make_ref_cl_golden.py)."""
+    z = np.load(REF_CL)
+    return [{k: z[f"{name}/{k}"] for k in ("box", "gravity", "pos", "vel", "rho", "p", "acc")} | {"name": str(name)}
+            for name in z["names"]]
+
+
+def interior(pos, box, margin=0.0101):
+    """Particles farther than the wall radius (0.01 m) from every wall: no wall term acts on them."""
+    half = np.asarray(box, np.float64) / 2
+    return np.all(np.abs(np.asarray(pos, np.float64)) < half - margin, axis=1)
+
+
+def test_ref_cl_golden_reproduces(oracle_mod):
+    """Where the reference tree is present, its kernels rebuilt here give the committed bits."""
+    O = oracle_mod
+    if O.build_ref() is None or O.ref_lib() is None:
+        pytest.skip("the reference's kernels build only where the reference tree is present")
+    for c in ref_cl_cases():
+        rho, p, acc = O.ref_density_forces(c["pos"], c["vel"], c["box"], c["gravity"])
+        assert np.array_equal(rho, c["rho"]) and np.array_equal(p, c["p"]) and np.array_equal(acc, c["acc"]), c["name"]
+
+
+@pytest.mark.parametrize("case", ref_cl_cases(), ids=lambda c: c["name"])
+def test_oracle_matches_reference_kernels(oracle_mod, case):
+    """The oracle's density, pressure and (away from the walls) acceleration against the
+    reference's own OpenCL kernels on the same state, within the 1e-5 parity band. The kernels
+    sum in another order (x outer) and in float throughout, so agreement is at FP32 noise."""
+    O = oracle_mod
+    o = O.Oracle(tuple(case["box"]), O.REF, threads=4, gravity=case["gravity"])
+    o.add(case["pos"], case["vel"])
+    o.update_grid()
+    o.density()
+    o.forces()
+    s = o.state()
+    inside = interior(case["pos"], case["box"])
+    assert inside.sum() > 0.5 * len(inside)
+    errs = rel_errors({"rho": case["rho"], "p": case["p"]}, s)
+    errs.update(rel_errors({"acc": case["acc"][inside]},
+                           {"rho": s["rho"][inside], "acc": s["acc"][inside], "ascale": s["ascale"][inside]}))
+    assert_within(errs, case["name"])
+    # well inside the band: the two differ only by FP32 rounding and summation order
+    assert max(errs.values()) < 0.5, errs
