@@ -52,7 +52,7 @@ def build_ref(force=False):
     """Compile oracle/ref_cl/ref_cl.cpp, which includes sph_common.cl and sph_grid.cl from the
     reference tree where they lie, into oracle/_ref/librefcl.so. Returns the path, or None when
     the reference tree is absent."""
-    srcs = [os.path.join(REF_KERNELS, f) for f in ("sph_common.cl", "sph_grid.cl")]
+    srcs = [os.path.join(REF_KERNELS, f) for f in ("sph_common.cl", "sph_grid.cl", "sph_brute.cl")]
     if not all(os.path.exists(f) for f in srcs):
         return None
     here = os.path.join(HERE, "ref_cl")
@@ -81,6 +81,8 @@ def ref_lib():
         fp = ctypes.POINTER(ctypes.c_float)
         L.refcl_density_forces.argtypes = [ctypes.c_int, fp, fp, fp, fp, fp, fp, fp]
         L.refcl_density_forces.restype = ctypes.c_int
+        L.refcl_brute_density_forces.argtypes = [ctypes.c_int, fp, fp, fp, fp, fp, fp]
+        L.refcl_brute_density_forces.restype = ctypes.c_int
         _ref = L
     return _ref
 
@@ -100,6 +102,22 @@ def ref_density_forces(pos, vel, box, gravity):
     rc = L.refcl_density_forces(n, _f(pos), _f(vel), _f(b), _f(g), _f(rho), _f(p), _f(acc))
     if rc:
         raise ValueError("refcl_density_forces failed")
+    return rho, p, acc
+
+
+def ref_brute_density_forces(pos, vel, gravity):
+    """The reference's all-pairs density_pressure_step and forces_step (sph_brute.cl) for one
+    state: (rho, p, acc before the walls), in input order."""
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("reference kernels not built (oracle.build_ref)")
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    vel = np.ascontiguousarray(vel, np.float32).reshape(-1, 3)
+    n = pos.shape[0]
+    g = np.ascontiguousarray(gravity, np.float32)
+    rho, p, acc = np.zeros(n, np.float32), np.zeros(n, np.float32), np.zeros((n, 3), np.float32)
+    if L.refcl_brute_density_forces(n, _f(pos), _f(vel), _f(g), _f(rho), _f(p), _f(acc)):
+        raise ValueError("refcl_brute_density_forces failed")
     return rho, p, acc
 
 

@@ -21,9 +21,10 @@
 #define CLK_LOCAL_MEM_FENCE 1
 #define CLK_GLOBAL_MEM_FENCE 2
 
-// Everything below, and the kernel sources, live in namespace clk so that the OpenCL
-// built-ins (sqrt, pow, floor, dot) do not meet the C++ library's overloads.
-namespace clk {
+// The types and built-ins live in namespace clt, which the harness's kernel namespaces use:
+// the OpenCL built-ins (sqrt, pow, floor, dot) then never meet the C++ library's overloads,
+// and argument-dependent lookup on the vector types finds no kernel function.
+namespace clt {
 
 typedef unsigned int uint;
 
@@ -89,6 +90,6 @@ inline int atomic_inc(volatile int *p)
     return old;
 }
 
-}  // namespace clk
+}  // namespace clt
 
 #endif  // CL_SHIM_H

@@ -6,7 +6,8 @@ on machines without the reference tree.
     python tests/golden/make_ref_cl_golden.py
 
 Each case: a box, gravity, a state (positions, velocities) reached by stepping the oracle
-from a seeded scene, and the kernels' density, pressure and acceleration (before the walls).
+from a seeded scene, and the kernels' density, pressure and acceleration (before the walls);
+for the 0.4 m dam break also those of the all-pairs kernels (sph_brute.cl).
 """
 import os
 import sys
@@ -56,6 +57,11 @@ def main():
         out[name + "/rho"] = rho
         out[name + "/p"] = p
         out[name + "/acc"] = acc
+        if kind == "reference":  # the all-pairs kernels (sph_brute.cl) on the small scenes
+            rb, pb, ab = O.ref_brute_density_forces(st["pos"], st["vel"], g)
+            out[name + "/brute_rho"] = rb
+            out[name + "/brute_p"] = pb
+            out[name + "/brute_acc"] = ab
     np.savez_compressed(OUT, names=np.array([c[0] for c in CASES]), **out)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 

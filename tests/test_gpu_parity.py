@@ -272,7 +272,7 @@ def test_gpu_matches_reference_kernels(sphlib, oracle_mod):
         o.step(1)
         s = o.state()  # the per-particle force scale A
         inside = interior(c["pos"], box)
-        errs = rel_errors({"rho": got["rho"], "p": got["p"]}, {"rho": c["rho"], "p": c["p"]})
+        errs = rel_errors({"rho": got["rho"], "p": got["p"]}, {"rho": c["rho"], "p": c["p"], "ascale": s["ascale"]})
         errs.update(rel_errors({"acc": got["acc"][inside]},
                                {"rho": c["rho"][inside], "acc": c["acc"][inside], "ascale": s["ascale"][inside]}))
         assert_within(errs, c["name"])

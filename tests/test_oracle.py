@@ -207,8 +207,8 @@ def ref_cl_cases():
     """Golden outputs of the reference's OpenCL density_pressure_step and forces_step
     (resources/kernels/sph_grid.cl) compiled for the CPU (tests/golden/make_ref_cl_golden.py)."""
     z = np.load(REF_CL)
-    return [{k: z[f"{name}/{k}"] for k in ("box", "gravity", "pos", "vel", "rho", "p", "acc")} | {"name": str(name)}
-            for name in z["names"]]
+    keys = ("box", "gravity", "pos", "vel", "rho", "p", "acc", "brute_rho", "brute_p", "brute_acc")
+    return [{k: z[f"{name}/{k}"] for k in keys if f"{name}/{k}" in z} | {"name": str(name)} for name in z["names"]]
 
 
 def interior(pos, box, margin=0.0101):
@@ -225,6 +225,9 @@ def test_ref_cl_golden_reproduces(oracle_mod):
     for c in ref_cl_cases():
         rho, p, acc = O.ref_density_forces(c["pos"], c["vel"], c["box"], c["gravity"])
         assert np.array_equal(rho, c["rho"]) and np.array_equal(p, c["p"]) and np.array_equal(acc, c["acc"]), c["name"]
+        if "brute_rho" in c:
+            rho, p, acc = O.ref_brute_density_forces(c["pos"], c["vel"], c["gravity"])
+            assert np.array_equal(rho, c["brute_rho"]) and np.array_equal(acc, c["brute_acc"]), c["name"]
 
 
 @pytest.mark.parametrize("case", ref_cl_cases(), ids=lambda c: c["name"])
@@ -247,3 +250,28 @@ def test_oracle_matches_reference_kernels(oracle_mod, case):
     assert_within(errs, case["name"])
     # well inside the band: the two differ only by FP32 rounding and summation order
     assert max(errs.values()) < 0.5, errs
+
+
+@pytest.mark.parametrize("case", [c for c in ref_cl_cases() if "brute_rho" in c], ids=lambda c: c["name"])
+def test_oracle_brute_matches_reference_brute_kernels(oracle_mod, case):
+    """The oracle's all-pairs restatement against the reference's own all-pairs kernels
+    (sph_brute.cl) on the same state: density and pressure everywhere, acceleration away from
+    the walls. Both evaluate in float, in the same order, so the gap is library rounding only."""
+    O = oracle_mod
+    o = O.Oracle(tuple(case["box"]), O.CANON, threads=4, gravity=case["gravity"])
+    o.add(case["pos"], case["vel"])
+    o.brute_step()
+    s = o.state()
+    g = O.Oracle(tuple(case["box"]), O.REF, threads=4, gravity=case["gravity"])
+    g.add(case["pos"], case["vel"])
+    g.update_grid()
+    g.density()
+    g.forces()
+    A = g.state()["ascale"]  # the per-particle force scale
+    inside = interior(case["pos"], case["box"])
+    errs = rel_errors({"rho": s["rho"], "p": s["p"]}, {"rho": case["brute_rho"], "p": case["brute_p"], "ascale": A})
+    errs.update(rel_errors({"acc": s["acc"][inside]},
+                           {"rho": case["brute_rho"][inside], "acc": case["brute_acc"][inside],
+                            "ascale": A[inside]}))
+    assert_within(errs, case["name"])
+    assert max(errs.values()) < 0.1, errs
