@@ -1013,6 +1013,36 @@ int sph_export_positions(sph_ctx *c, float *dev_xyz, float *dev_vel, void *consu
     }
 }
 
+int sph_splat(sph_ctx *c, uint32_t scene, int32_t axis, uint32_t width, uint32_t height, uint32_t *dev_count,
+              float *dev_depth, void *consumer_stream)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (scene >= c->sc.size()) return fail(c, SPH_ERR_ARG, "scene index out of range");
+    if (axis < 0 || axis > 2) return fail(c, SPH_ERR_ARG, "axis must be 0, 1 or 2");
+    if (width == 0 || height == 0 || (uint64_t) width * height > (1ull << 28))
+        return fail(c, SPH_ERR_ARG, "image size must be in [1, 2^28] pixels");
+    if (!dev_count && !dev_depth) return fail(c, SPH_ERR_ARG, "no output image");
+    if (c->state == EMPTY) return fail(c, SPH_ERR_STATE, "nothing uploaded");
+    CK(c, cudaSetDevice(c->device));
+    const int au = axis == 0 ? 1 : 0, av = axis == 2 ? 1 : 2;
+    const SceneHost &h = c->sc[scene];
+    const float half_u = h.box[au] / 2.0f, half_v = h.box[av] / 2.0f;
+    const float scale_u = (float) width / h.box[au], scale_v = (float) height / h.box[av];
+    const int layout_sorted = (c->state == SORTED || c->state == DENSE) ? 1 : 0;
+    if (is_f64(c))
+        CK(c, launch_splat<double>(c->b, c->n, layout_sorted, scene, axis, half_u, half_v, scale_u, scale_v, width,
+                                   height, dev_count, dev_depth, c->stream));
+    else
+        CK(c, launch_splat<float>(c->b, c->n, layout_sorted, scene, axis, half_u, half_v, scale_u, scale_v, width,
+                                  height, dev_count, dev_depth, c->stream));
+    if (consumer_stream) {
+        if (!c->ho_export) CK(c, cudaEventCreateWithFlags(&c->ho_export, cudaEventDisableTiming));
+        CK(c, cudaEventRecord(c->ho_export, c->stream));
+        CK(c, cudaStreamWaitEvent((cudaStream_t) consumer_stream, c->ho_export, 0));
+    }
+    return SPH_OK;
+}
+
 int sph_download(sph_ctx *c, float *xyz, float *vel, float *rho, float *p, float *acc)
 {
     try {

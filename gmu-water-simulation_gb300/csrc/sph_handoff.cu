@@ -36,7 +36,71 @@ cudaError_t launch_handoff(const DevBufs &b, uint32_t n, int layout_sorted, floa
     return cudaGetLastError();
 }
 
+// Orthographic point splat of one scene along axis `a` onto a width x height image over the
+// box face: pixel (u, v) of a particle = floor((p + box/2) * (pixels / box)) per image axis in
+// explicitly rounded float, clamped to the image. Per pixel: the particle count and the
+// smallest coordinate along the axis (the particle nearest to a viewer on the -a side), as an
+// order-preserving integer so that atomicMin gives the same bits in any order.
+__device__ __forceinline__ uint32_t order_key(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) k_splat(const Vec4<R> *__restrict__ pos, uint32_t n, uint32_t scene, int a,
+                                               float half_u, float half_v, float scale_u, float scale_v,
+                                               uint32_t width, uint32_t height, uint32_t *__restrict__ count,
+                                               uint32_t *__restrict__ depth_key)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Vec4<R> p = ldc4(pos + i);
+    if (wbits(p.w) != scene) return;
+    const float c[3] = {(float) p.x, (float) p.y, (float) p.z};
+    const int au = a == 0 ? 1 : 0, av = a == 2 ? 1 : 2;
+    const float fu = floorf(__fmul_rn(__fadd_rn(c[au], half_u), scale_u));
+    const float fv = floorf(__fmul_rn(__fadd_rn(c[av], half_v), scale_v));
+    // NaN and values below the image go to pixel 0, values beyond it to the last pixel
+    const uint32_t u = fu >= (float) width ? width - 1 : (fu >= 0.0f ? (uint32_t) fu : 0u);
+    const uint32_t v = fv >= (float) height ? height - 1 : (fv >= 0.0f ? (uint32_t) fv : 0u);
+    const size_t pix = (size_t) v * width + u;
+    if (count) atomicAdd(count + pix, 1u);
+    if (depth_key) atomicMin(depth_key + pix, order_key(c[a]));
+}
+
+__global__ void k_splat_depth(uint32_t *__restrict__ key, size_t npix)
+{
+    const size_t k = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= npix) return;
+    const uint32_t b = key[k];
+    // back from the order-preserving key; an untouched pixel (all ones) becomes +inf
+    key[k] = b == 0xFFFFFFFFu ? 0x7F800000u : ((b & 0x80000000u) ? (b & 0x7FFFFFFFu) : ~b);
+}
+
+template <class R>
+cudaError_t launch_splat(const DevBufs &b, uint32_t n, int layout_sorted, uint32_t scene, int axis, float half_u,
+                         float half_v, float scale_u, float scale_v, uint32_t width, uint32_t height,
+                         uint32_t *count, float *depth, cudaStream_t st)
+{
+    const size_t npix = (size_t) width * height;
+    cudaError_t e = cudaSuccess;
+    if (count) e = cudaMemsetAsync(count, 0, 4 * npix, st);
+    if (e == cudaSuccess && depth) e = cudaMemsetAsync(depth, 0xFF, 4 * npix, st);
+    if (e != cudaSuccess) return e;
+    const Vec4<R> *pos = (const Vec4<R> *) (layout_sorted ? b.pos_s : b.pos_u);
+    if (n)
+        k_splat<R><<<(n + 255) / 256, 256, 0, st>>>(pos, n, scene, axis, half_u, half_v, scale_u, scale_v, width,
+                                                   height, count, (uint32_t *) depth);
+    if (depth) k_splat_depth<<<(unsigned) ((npix + 255) / 256), 256, 0, st>>>((uint32_t *) depth, npix);
+    return cudaGetLastError();
+}
+
 template cudaError_t launch_handoff<float>(const DevBufs &, uint32_t, int, float *, float *, cudaStream_t);
 template cudaError_t launch_handoff<double>(const DevBufs &, uint32_t, int, float *, float *, cudaStream_t);
+template cudaError_t launch_splat<float>(const DevBufs &, uint32_t, int, uint32_t, int, float, float, float, float,
+                                         uint32_t, uint32_t, uint32_t *, float *, cudaStream_t);
+template cudaError_t launch_splat<double>(const DevBufs &, uint32_t, int, uint32_t, int, float, float, float, float,
+                                          uint32_t, uint32_t, uint32_t *, float *, cudaStream_t);
 
 }  // namespace sph

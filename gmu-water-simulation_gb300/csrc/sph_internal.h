@@ -149,6 +149,12 @@ cudaError_t launch_emit_fountain(uint64_t seed, uint32_t step, uint32_t n, const
 template <class R>
 cudaError_t launch_handoff(const DevBufs &b, uint32_t n, int layout_sorted, float *xyz, float *v, cudaStream_t st);
 
+// orthographic point splat of one scene into per-pixel counts and nearest depth (sph_handoff.cu)
+template <class R>
+cudaError_t launch_splat(const DevBufs &b, uint32_t n, int layout_sorted, uint32_t scene, int axis, float half_u,
+                         float half_v, float scale_u, float scale_v, uint32_t width, uint32_t height,
+                         uint32_t *count, float *depth, cudaStream_t st);
+
 // mixed-precision passes (sph_mixed.cu)
 cudaError_t mixed_permute(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, cudaStream_t st);
 cudaError_t mixed_density(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, cudaStream_t st);

@@ -32,7 +32,7 @@ EXPORTS = (
     "sph_upload", "sph_append", "sph_emit_fountain", "sph_set_gravity", "sph_step", "sph_pass_grid", "sph_pass_density",
     "sph_pass_forces", "sph_pass_times", "sph_get_counts", "sph_num_scenes", "sph_num_particles",
     "sph_get_resolution", "sph_download", "sph_download_f64", "sph_handoff_async", "sph_handoff_ready",
-    "sph_handoff_wait", "sph_export_positions", "sph_get_grid", "sph_stats",
+    "sph_handoff_wait", "sph_export_positions", "sph_splat", "sph_get_grid", "sph_stats",
     "sph_scene_reference_dam_break", "sph_scene_lattice", "sph_scene_batch_plan", "sph_scene_fountain_emit",
 )
 
@@ -107,6 +107,7 @@ def load(path=None):
         "sph_handoff_ready": (i32, [vp]),
         "sph_handoff_wait": (i32, [vp]),
         "sph_export_positions": (i32, [vp, vp, vp, vp]),
+        "sph_splat": (i32, [vp, u32, i32, u32, u32, vp, vp, vp]),
         "sph_get_grid": (i32, [vp, up, up, up]),
         "sph_stats": (i32, [vp, u32, dp]),
         "sph_scene_reference_dam_break": (ctypes.c_int64, [f, fp, ctypes.c_uint64]),
@@ -372,6 +373,24 @@ class SphContext:
                                              ctypes.c_void_p(dev_vel_ptr) if dev_vel_ptr else None,
                                              ctypes.c_void_p(consumer_stream) if consumer_stream else None))
 
+    def splat_raw(self, scene, axis, width, height, dev_count_ptr, dev_depth_ptr, consumer_stream=None):
+        """Point splat into device images at raw pointers (see sph_splat)."""
+        self._ck(load().sph_splat(self.h, scene, axis, width, height,
+                                  ctypes.c_void_p(dev_count_ptr) if dev_count_ptr else None,
+                                  ctypes.c_void_p(dev_depth_ptr) if dev_depth_ptr else None,
+                                  ctypes.c_void_p(consumer_stream) if consumer_stream else None))
+
+    def splat(self, scene, axis, width, height):
+        """(counts, depth) images of one scene as (height, width) numpy arrays; the device
+        buffers are torch tensors (device memory plumbing only)."""
+        import torch
+
+        cnt = torch.empty((height, width), dtype=torch.int32, device="cuda")
+        dep = torch.empty((height, width), dtype=torch.float32, device="cuda")
+        s = torch.cuda.current_stream()
+        self.splat_raw(scene, axis, width, height, cnt.data_ptr(), dep.data_ptr(), s.cuda_stream)
+        return cnt.cpu().numpy().view(np.uint32), dep.cpu().numpy()
+
     def grid(self):
         """(cell of each particle, count of each cell, sorted ids) of the last grid pass."""
         n = self.n
@@ -388,6 +407,18 @@ class SphContext:
         self._ck(load().sph_stats(self.h, scene, _p(out, ctypes.c_double)))
         return {"mass": out[0], "momentum": out[1:4].copy(), "kinetic": out[4], "rho_mean": out[5],
                 "rho_max": out[6], "count": int(out[7])}
+
+
+def write_pgm(path, image, vmax=None):
+    """An image (row 0 at the smallest coordinate) as an 8-bit binary PGM, row 0 at the bottom."""
+    a = np.asarray(image, np.float64)
+    a = np.where(np.isfinite(a), a, 0.0)
+    top = float(vmax if vmax is not None else (a.max() if a.size and a.max() > 0 else 1.0))
+    g = np.clip(np.round(a / top * 255.0), 0, 255).astype(np.uint8)[::-1]
+    with open(path, "wb") as f:
+        f.write(f"P5\n{g.shape[1]} {g.shape[0]}\n255\n".encode())
+        f.write(g.tobytes())
+    return path
 
 
 # ----------------------------------------------------------------- reference-shaped simulator

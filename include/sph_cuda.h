@@ -211,6 +211,16 @@ int sph_handoff_wait(sph_ctx *ctx);
  * into CUDA. Queued on the context's stream; consumer_stream (a cudaStream_t, or NULL) is made
  * to wait for it. */
 int sph_export_positions(sph_ctx *ctx, float *dev_xyz, float *dev_vel, void *consumer_stream);
+/* Headless point splat of one scene, for a front end without a graphics API: an orthographic
+ * view along `axis` (0 = x, 1 = y, 2 = z) onto a width x height image covering the box face
+ * spanned by the other two axes in increasing order (u, v); row-major, row 0 at the smallest
+ * v. A particle lands in pixel floor((p + box/2) * (pixels / box)) per image axis (float,
+ * clamped to the image). dev_count (width*height, may be NULL): particles per pixel.
+ * dev_depth (width*height floats, may be NULL): the smallest coordinate along axis in the
+ * pixel (the particle nearest a viewer on the negative side), +inf where there is none.
+ * Deterministic. Queued on the context's stream; consumer_stream (or NULL) waits for it. */
+int sph_splat(sph_ctx *ctx, uint32_t scene, int32_t axis, uint32_t width, uint32_t height, uint32_t *dev_count,
+              float *dev_depth, void *consumer_stream);
 
 /* The grid of the last grid pass: the cell of every particle (scene-major, id order,
  * cell index local to its scene: x + y*X + z*X*Y), the count of every cell (scene-major),

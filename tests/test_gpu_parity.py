@@ -368,6 +368,39 @@ def test_handoff_and_export(sphlib, prec):
     b.close()
 
 
+def test_splat_counts_and_depth(sphlib, tmp_path):
+    """The point splat equals a numpy restatement of its pixel mapping (float32 add and
+    multiply, floor, clamp) bit for bit, per axis, for one scene of a batch."""
+    boxes = [(1.0, 1.0, 0.5), (0.6, 0.8, 0.7)]
+    parts = [c0_scene(sphlib, dims=(16, 16, 16)), sphlib.dam_break_scene((9, 12, 10), boxes[1], 5)]
+    counts = [q.shape[0] for q in parts]
+    ctx = sphlib.SphContext(boxes, counts, gravity=G981)
+    ctx.upload(np.concatenate(parts), None, counts)
+    ctx.step(7)
+    d = ctx.download()
+    for scene in (0, 1):
+        p = d["pos"][sum(counts[:scene]):sum(counts[:scene + 1])]
+        box = np.asarray(boxes[scene], np.float32)
+        for axis, (W, H) in zip((0, 1, 2), ((40, 30), (64, 48), (33, 77))):
+            cnt, dep = ctx.splat(scene, axis, W, H)
+            au, av = (1, 2) if axis == 0 else ((0, 2) if axis == 1 else (0, 1))
+            fu = np.floor((p[:, au] + box[au] / np.float32(2)) * (np.float32(W) / box[au]))
+            fv = np.floor((p[:, av] + box[av] / np.float32(2)) * (np.float32(H) / box[av]))
+            u = np.clip(np.nan_to_num(fu, nan=0.0), 0, W - 1).astype(np.int64)
+            v = np.clip(np.nan_to_num(fv, nan=0.0), 0, H - 1).astype(np.int64)
+            want = np.zeros((H, W), np.uint32)
+            np.add.at(want, (v, u), 1)
+            wdep = np.full((H, W), np.inf, np.float32)
+            np.minimum.at(wdep, (v, u), p[:, axis])
+            assert np.array_equal(cnt, want), (scene, axis)
+            assert np.array_equal(dep, wdep), (scene, axis)
+            assert int(cnt.sum()) == counts[scene]
+    path = sphlib.write_pgm(str(tmp_path / "splat.pgm"), cnt)
+    raw = open(path, "rb").read()
+    assert raw.startswith(b"P5\n33 77\n255\n") and len(raw) == len(b"P5\n33 77\n255\n") + 33 * 77
+    ctx.close()
+
+
 def test_device_emitter_equals_host_emitter(sphlib):
     """sph_emit_fountain generates on the device the same bits as the host generator, and a run
     fed by it equals a run fed by sph_append of the host-generated particles."""
