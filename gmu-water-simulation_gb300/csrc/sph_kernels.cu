@@ -850,21 +850,6 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
         k_forces_mask<R, 0><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
                                                           b.masks, po, vo, ao, b.cid_u, b.count);
         break;
-    case 3:
-        k_forces_mask<R, 0><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
-                                                          b.masks, po, vo, ao, b.cid_u, b.count);
-        break;
-    case 8:
-        k_forces_flat<R, 24><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
-                                                           b.masks, po, vo, ao, b.cid_u, b.count);
-        break;
-    case 7: {
-        constexpr size_t smem = stage_smem_bytes<R>();
-        static_assert(smem <= 48 * 1024, "the staging buffer fits the default dynamic shared memory limit");
-        k_forces_stage<R><<<nblk(n, 256), 256, smem, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
-                                                           b.masks, po, vo, ao, b.cid_u, b.count);
-        break;
-    }
     case 4:
         k_forces_mask<R, 4><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
                                                           b.masks, po, vo, ao, b.cid_u, b.count);
