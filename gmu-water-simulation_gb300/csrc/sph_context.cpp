@@ -208,6 +208,7 @@ int allocate(sph_ctx *c)
         {(void **) &b.stats, 64 * c->sc.size()},
         {(void **) &b.stats_partial, 6 * 8 * 64 * c->sc.size()},
         {(void **) &b.masks, 4 * 36 * N},
+        {(void **) &b.frec, mixed ? 0 : 2 * r4 * N},
     };
     size_t total = 0;
     for (auto &it : items) total += (it.bytes + 255) & ~size_t(255);
@@ -417,7 +418,7 @@ int build_graph(sph_ctx *c, int steps)
 }
 
 bool valid_density(int v) { return v == 0 || v == 1 || v == 2 || v == 4; }
-bool valid_forces(int v) { return v >= 0 && v <= 6; }
+bool valid_forces(int v) { return v >= 0 && v <= 7; }
 
 int bucket_of(uint64_t n)
 {
@@ -807,6 +808,7 @@ int sph_autotune(sph_ctx *c, int32_t reps)
     cfgs.push_back({0, 4});
     cfgs.push_back({0, 5});
     cfgs.push_back({0, 6});
+    cfgs.push_back({0, 7});
     float best = 1e30f;
     int bd = c->tune.density_p, bf = c->tune.forces_mode;
     for (const Cfg &g : cfgs) {

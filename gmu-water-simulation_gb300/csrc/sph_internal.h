@@ -62,6 +62,7 @@ struct DevBufs {
     double *stats;         // per-scene FP64 reductions, 8 doubles each
     double *stats_partial; // per-scene slices of the reductions (kSplit x 6 doubles each)
     uint32_t *masks;       // accepted-neighbour bit masks of the density pass, 36 words per particle
+    void *frec;            // force records of the density pass (variant 7): (x, y, z, p/rho^2), (v, 1/rho)
     // mixed-precision form only
     void *lo_s, *lo_u;     // low parts of the hi/lo positions (float4, .w unused)
     uint2 *gpos;           // gathered positions: 16-bit codes x | y << 16, z (sorted order)
@@ -113,7 +114,8 @@ struct MixConsts {
 //               of 32/64 entries per thread in shared memory; 3..7 = driven by the neighbour
 //               masks that the density pass then writes (density_p is ignored): 3/4 one
 //               neighbour per iteration without/with a 64-register cap, 5/6 two per
-//               iteration with/without it
+//               iteration with/without it, 7 as 6 with each neighbour's terms read from one
+//               packed force record (two 16-byte loads from one 32-byte record)
 struct Tune {
     static constexpr int ALL_PAIRS = 16;  // both passes over every particle of the scene
     int density_p = 2;

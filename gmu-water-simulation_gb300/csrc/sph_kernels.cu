@@ -344,11 +344,12 @@ __global__ void __launch_bounds__(BLOCK) k_forces_list(
 // set = candidate window_start + 32 w + k is a neighbour (self included). Candidates past
 // MASK_WORDS chunks are not recorded: the force pass tests them itself.
 
-template <class R>
+template <class R, bool REC>
 __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
                                                       const uint32_t *__restrict__ start,
                                                       const SceneDev *__restrict__ scenes, uint32_t n, Consts<R> c,
-                                                      uint32_t *__restrict__ masks)
+                                                      uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ vel,
+                                                      Vec4<R> *__restrict__ frec)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -389,7 +390,13 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
     }
     const R rho = rmul(rmul(acc, c.c_poly6), c.mass);
     const R p = rmul(c.k, rsub(rho, c.rho0));
-    st4(aux + i, Vec4<R>{rho, p, rdiv(p, rmul(rho, rho)), rdiv((R) 1, rho)});
+    const R q = rdiv(p, rmul(rho, rho)), inv = rdiv((R) 1, rho);
+    st4(aux + i, Vec4<R>{rho, p, q, inv});
+    if (REC) {  // the force pass's view of this particle as a neighbour, in one 2 x 16-byte record
+        const Vec4<R> vi = ld4(vel + i);
+        st4(frec + 2 * (size_t) i, Vec4<R>{pi.x, pi.y, pi.z, q});
+        st4(frec + 2 * (size_t) i + 1, Vec4<R>{vi.x, vi.y, vi.z, inv});
+    }
 }
 
 // Forces driven by the density pass's masks: only accepted neighbours are visited, in the
@@ -452,13 +459,13 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask(
 // loaded before either's terms are added, so two gathers are in flight at once and the loop
 // overhead is paid once per pair. The terms are still added one neighbour at a time in
 // candidate order (the sums are the same bits as the other forms).
-template <class R, int MINB>
+template <class R, int MINB, bool REC>
 __global__ void __launch_bounds__(256, MINB) k_forces_mask2(
     const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
     const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
-    uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, Vec4<R> *__restrict__ pos_out,
-    Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out, uint2 *__restrict__ cid_out,
-    uint32_t *__restrict__ count)
+    uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ frec,
+    Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out,
+    uint2 *__restrict__ cid_out, uint32_t *__restrict__ count)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -501,11 +508,20 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask2(
                     const bool two = m != 0;
                     const uint32_t j1 = two ? cb + (uint32_t) (__ffs(m) - 1) : j0;
                     m &= m - 1;
-                    const Vec4<R> p0 = ld4(pos + j0), v0 = ld4(vel + j0);
-                    const Vec4<R> p1 = ld4(pos + j1), v1 = ld4(vel + j1);
+                    Vec4<R> p0, v0, p1, v1;
                     R q0, inv0, q1, inv1;
-                    ld_qinv(aux + j0, q0, inv0);
-                    ld_qinv(aux + j1, q1, inv1);
+                    if (REC) {
+                        p0 = ld4(frec + 2 * (size_t) j0);
+                        v0 = ld4(frec + 2 * (size_t) j0 + 1);
+                        p1 = ld4(frec + 2 * (size_t) j1);
+                        v1 = ld4(frec + 2 * (size_t) j1 + 1);
+                        q0 = p0.w, inv0 = v0.w, q1 = p1.w, inv1 = v1.w;
+                    } else {
+                        p0 = ld4(pos + j0), v0 = ld4(vel + j0);
+                        p1 = ld4(pos + j1), v1 = ld4(vel + j1);
+                        ld_qinv(aux + j0, q0, inv0);
+                        ld_qinv(aux + j1, q1, inv1);
+                    }
                     pair_terms<R>(pi, vi, qi, p0, v0, q0, inv0, c, fpx, fpy, fpz, fvx, fvy, fvz);
                     if (two) pair_terms<R>(pi, vi, qi, p1, v1, q1, inv1, c, fpx, fpy, fpz, fvx, fvy, fvz);
                 }
@@ -821,8 +837,14 @@ cudaError_t Launch<R>::density(const DevBufs &b, uint32_t n, Consts<R> c, const 
         k_density_all<R><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c);
         return cudaGetLastError();
     }
+    if (t.forces_mode == 7) {  // masks and force records
+        k_density_mask<R, true><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c, b.masks,
+                                                              (const Vec4<R> *) b.vel_s, (Vec4<R> *) b.frec);
+        return cudaGetLastError();
+    }
     if (t.forces_mode >= 3) {  // the mask-driven force passes need the masks
-        k_density_mask<R><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c, b.masks);
+        k_density_mask<R, false><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c, b.masks, nullptr,
+                                                               nullptr);
         return cudaGetLastError();
     }
     switch (t.density_p) {
@@ -855,12 +877,17 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
                                                           b.masks, po, vo, ao, b.cid_u, b.count);
         break;
     case 5:
-        k_forces_mask2<R, 4><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
-                                                           b.masks, po, vo, ao, b.cid_u, b.count);
+        k_forces_mask2<R, 4, false><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n,
+                                                                  c, b.masks, nullptr, po, vo, ao, b.cid_u, b.count);
         break;
     case 6:
-        k_forces_mask2<R, 0><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
-                                                           b.masks, po, vo, ao, b.cid_u, b.count);
+        k_forces_mask2<R, 0, false><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n,
+                                                                  c, b.masks, nullptr, po, vo, ao, b.cid_u, b.count);
+        break;
+    case 7:
+        k_forces_mask2<R, 0, true><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
+                                                                 b.masks, (const Vec4<R> *) b.frec, po, vo, ao,
+                                                                 b.cid_u, b.count);
         break;
     case 1:
         k_forces_list<R, 32, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,

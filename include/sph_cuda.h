@@ -165,7 +165,8 @@ int sph_pass_times(sph_ctx *ctx, double ms[5]);
  *            3, 4 = the density pass records each particle's accepted neighbours as bit masks
  *            per row and the force pass visits only those (density_variant is then unused);
  *            4 trades registers for occupancy differently from 3; 5 and 6 load two accepted
- *            neighbours per iteration (with and without the register cap of 4) */
+ *            neighbours per iteration (with and without the register cap of 4); 7 is 6 reading each
+ *            neighbour from one packed 32-byte force record written by the density pass */
 int sph_set_variant(sph_ctx *ctx, int32_t density_variant, int32_t forces_variant);
 int sph_get_variant(const sph_ctx *ctx, int32_t out[2]);
 
