@@ -67,10 +67,13 @@ def grid_cells(box):
     return int(np.prod([int(np.ceil(np.float32(b) / H32)) for b in box]))
 
 
-def alg_bytes(N, C, rs=4):
+def alg_bytes(N, C, rs=4, forces_variant=4):
     """Compulsory DRAM bytes of each kernel of one step: every array it must touch,
-    read or written once (neighbour re-reads are cache hits). rs = bytes per real."""
+    read or written once (neighbour re-reads are cache hits). rs = bytes per real.
+    Force variant 7 also has the density pass read velocities and write the packed force
+    records, which the force pass then reads."""
     r4 = 4 * rs
+    rec = 3 * r4 * N if forces_variant == 7 else 0  # velocity read + 2 x r4 record written
     return {
         # counts read twice, starts/cursors written, counts zeroed
         "scan": 20 * C,
@@ -80,19 +83,21 @@ def alg_bytes(N, C, rs=4):
         "rank_permute": 8 * N + 4 * N + 4 * r4 * N + 4 * C,
         # sorted positions read, (rho, p, p/rho^2, 1/rho) written, row starts; the mask form
         # also writes the neighbour masks (one word per row at rest density: 36 B)
-        "density": r4 * N + r4 * N + 4 * C + MASK_BYTES * N,
+        "density": r4 * N + r4 * N + 4 * C + MASK_BYTES * N + rec,
         # own position, velocity, aux read; new position, velocity, (cell, id) written;
         # row starts read; counts read-modify-write; the mask form reads the masks
-        "forces": 3 * r4 * N + 2 * r4 * N + 8 * N + 12 * C + MASK_BYTES * N,
+        "forces": 3 * r4 * N + 2 * r4 * N + 8 * N + 12 * C + MASK_BYTES * N + (2 * rec) // 3,
     }
 
 
 MASK_BYTES = 36  # 9 rows x one 32-bit mask word per particle (rest density)
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernels,
-# from one ncu capture of an early step of this workload (L2 flushed before each replay);
-# profiles/step_kernels_dam_break_1m.md
-TRAFFIC = {"k_forces": 102.44e6, "k_density": 21.43e6}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernels
+# per force variant, from one ncu capture of an early step of this workload (L2 flushed before
+# each replay); profiles/step_kernels_dam_break_1m.md (variant 4) and
+# profiles/k_density_mask_k_forces_mask2_records_dam_break_1m.md (variant 7)
+TRAFFIC = {("k_forces", 4): 102.44e6, ("k_density", 4): 21.43e6,
+           ("k_forces", 7): 133.90e6, ("k_density", 7): 58.08e6}
 
 
 def load_peak():
@@ -360,6 +365,8 @@ def run_config(args):
         return work
 
     variant = ctx.autotune(reps=2) if ctx.n else (0, 3)
+    if args.form != "mixed":
+        ctx.set_online_tuning(50)
     warm = []
     advance(max(args.warmup, 3), warm)
     ms = []
@@ -422,14 +429,21 @@ def main():
         variant = ctx.variant()
     else:
         variant = ctx.autotune(reps=3)
+        # the state changes over the run (the column compresses): re-time the mask-driven force
+        # variants every 50 steps on real steps (all give the same bits)
+        if args.form != "mixed":
+            ctx.set_online_tuning(50)
     ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    used = []  # force variant of each timed step (online tuning may change it)
 
     def one_step(evs=None):
         if evs is not None:
             evs[0].record(ext)
         ctx.pass_grid()
         if evs is not None:
+            used.append(ctx.variant()[1])
             evs[1].record(ext)
         ctx.pass_density()
         if evs is not None:
@@ -468,13 +482,16 @@ def main():
     resident_final = ctx.download()
     fp64_check = fp64_error(sphcuda, ctx, form, N)
 
-    ab = alg_bytes(N, C, rs)
+    # bytes of each timed step by the variant it ran, against the summed event times
+    ab_steps = [alg_bytes(N, C, rs, v) for v in used]
+    ab = {k: sum(a[k] for a in ab_steps) / len(ab_steps) for k in ab_steps[0]}
+    main_v = max(set(used), key=used.count)
     peak, peak_src = load_peak()
     mean = lambda xs: sum(xs) / len(xs)
     dom = "forces" if mean(forc_ms) >= mean(dens_ms) else "density"
     dom_ms = mean(forc_ms) if dom == "forces" else mean(dens_ms)
     achieved = ab[dom] / (dom_ms / 1000.0) / 1e9
-    traffic = TRAFFIC.get(f"k_{dom}") if args.form == "plain" and not args.variant else None
+    traffic = TRAFFIC.get((f"k_{dom}", main_v)) if args.form == "plain" else None
     step_bytes = sum(ab.values())
 
     # ---- end to end through the C ABI with pinned host buffers, the same state sequence:
@@ -530,8 +547,10 @@ def main():
         "e2e": e2e,
         "cpu_baseline": cpu,
         "gpu_launches": KERNELS_PER_STEP * args.steps,
-        "launch_variant": {"density": variant[0], "forces": variant[1],
-                           "picked_by": "--variant" if args.variant else "sph_autotune"},
+        "launch_variant": {"density": variant[0], "forces": main_v,
+                           "forces_steps": {str(v): used.count(v) for v in sorted(set(used))},
+                           "picked_by": "--variant" if args.variant else
+                           "sph_autotune, then online tuning every 50 steps"},
         "clocks": clk,
         "wall_s_timed_region": t_wall,
     }

@@ -68,6 +68,13 @@ struct sph_ctx {
     cudaEvent_t ho_ready = nullptr, ho_done = nullptr, ho_export = nullptr;
     float *ho_xyz = nullptr, *ho_vel = nullptr;
     bool ho_recorded = false;  // ho_done has been recorded at least once
+    // online tuning of the mask-driven force variant (sph_set_online_tuning)
+    int online_period = 0;     // steps between trials; 0 = off
+    uint64_t steps_run = 0;    // whole steps run by this context
+    int trial = -1;            // candidate being timed in this step, -1 = none
+    float trial_ms[3] = {0, 0, 0};
+    cudaEvent_t on_ev[2] = {nullptr, nullptr};
+    int graph_forces = -1;     // force variant captured in the graph
 };
 
 namespace {
@@ -414,6 +421,53 @@ int build_graph(sph_ctx *c, int steps)
     }
     c->graph_steps = steps;
     c->graph_n = c->n;
+    c->graph_forces = c->tune.forces_mode;
+    return SPH_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) ms = 0;
+    return ms;
+}
+
+// ---- online tuning: the mask-driven force variants compute the same bits, so real steps can
+// try each in turn. Every online_period steps, one step runs with each candidate, timed from
+// the start of its grid pass to the end of its force pass; the fastest is kept until the next
+// trial. A trial step waits for its own end (one host synchronisation per candidate).
+constexpr int kOnlineCand[3] = {4, 6, 7};
+
+bool online_active(const sph_ctx *c)
+{
+    return c->online_period > 0 && !is_mixed(c) && c->tune.forces_mode >= 3 && c->tune.forces_mode <= 7;
+}
+
+// before a step: start a due trial and set this step's candidate
+int online_begin_step(sph_ctx *c)
+{
+    if (!online_active(c)) return SPH_OK;
+    if (c->trial < 0 && c->steps_run % (uint64_t) c->online_period == 0) c->trial = 0;
+    if (c->trial < 0) return SPH_OK;
+    c->tune.forces_mode = kOnlineCand[c->trial];
+    CK(c, cudaEventRecord(c->on_ev[0], c->stream));
+    return SPH_OK;
+}
+
+// after a step: time a trial step; after the last candidate keep the fastest
+int online_end_step(sph_ctx *c)
+{
+    c->steps_run++;
+    if (c->trial < 0 || !online_active(c)) return SPH_OK;
+    CK(c, cudaEventRecord(c->on_ev[1], c->stream));
+    CK(c, cudaEventSynchronize(c->on_ev[1]));
+    c->trial_ms[c->trial] = elapsed(c->on_ev[0], c->on_ev[1]);
+    if (++c->trial < 3) return SPH_OK;
+    int best = 0;
+    for (int k = 1; k < 3; k++)
+        if (c->trial_ms[k] < c->trial_ms[best]) best = k;
+    c->tune.forces_mode = kOnlineCand[best];
+    c->trial = -1;
     return SPH_OK;
 }
 
@@ -474,12 +528,6 @@ void tune_store(const std::string &key, int dv, int fv)
     if (f) f << key << " " << dv << " " << fv << "\n";
 }
 
-float elapsed(cudaEvent_t a, cudaEvent_t b)
-{
-    float ms = 0;
-    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) ms = 0;
-    return ms;
-}
 
 }  // namespace
 
@@ -539,7 +587,7 @@ void sph_destroy(sph_ctx *c)
     drop_graph(c);
     for (auto &ev : c->ev)
         if (ev) cudaEventDestroy(ev);
-    for (cudaEvent_t ev : {c->ho_ready, c->ho_done, c->ho_export})
+    for (cudaEvent_t ev : {c->ho_ready, c->ho_done, c->ho_export, c->on_ev[0], c->on_ev[1]})
         if (ev) cudaEventDestroy(ev);
     if (c->ho_stream) cudaStreamDestroy(c->ho_stream);
     if (c->ho_xyz) cudaFree(c->ho_xyz);
@@ -683,8 +731,10 @@ int sph_pass_grid(sph_ctx *c)
     if (!c) return SPH_ERR_ARG;
     CK(c, cudaSetDevice(c->device));
     const bool prof = (c->prm.flags & SPH_FLAG_PROFILE) != 0;
+    int rc = c->state == HASHED ? online_begin_step(c) : SPH_OK;
+    if (rc) return rc;
     if (prof) CK(c, cudaEventRecord(c->ev[0], c->stream));
-    int rc = pass_grid(c);
+    rc = pass_grid(c);
     if (!rc && prof) CK(c, cudaEventRecord(c->ev[1], c->stream));
     return rc;
 }
@@ -710,6 +760,7 @@ int sph_pass_forces(sph_ctx *c)
         c->ms[3] = 0;
         c->ms[4] = 0;
     }
+    if (!rc) rc = online_end_step(c);
     return rc;
 }
 
@@ -721,8 +772,10 @@ int sph_step(sph_ctx *c, int32_t nsteps)
     CK(c, cudaSetDevice(c->device));
     if (c->prm.flags & SPH_FLAG_PROFILE) {
         for (int k = 0; k < nsteps; k++) {
+            int rc = online_begin_step(c);
+            if (rc) return rc;
             CK(c, cudaEventRecord(c->ev[0], c->stream));
-            int rc = pass_grid(c);
+            rc = pass_grid(c);
             if (rc) return rc;
             CK(c, cudaEventRecord(c->ev[1], c->stream));
             rc = pass_density(c);
@@ -731,6 +784,8 @@ int sph_step(sph_ctx *c, int32_t nsteps)
             rc = pass_forces(c);
             if (rc) return rc;
             CK(c, cudaEventRecord(c->ev[3], c->stream));
+            rc = online_end_step(c);
+            if (rc) return rc;
         }
         if (nsteps > 0) {
             CK(c, cudaEventSynchronize(c->ev[3]));
@@ -744,24 +799,53 @@ int sph_step(sph_ctx *c, int32_t nsteps)
     }
     const int unroll = graph_unroll(c->n);
     int done = 0;
-    if (nsteps >= unroll) {
-        if (!c->graph || c->graph_steps != unroll || c->graph_n != c->n) {
-            int rc = build_graph(c, unroll);
+    while (done < nsteps) {
+        // trial steps of the online tuning run one by one, outside the graph
+        if (online_active(c) && (c->trial >= 0 || c->steps_run % (uint64_t) c->online_period == 0)) {
+            int rc = online_begin_step(c);
+            if (!rc) rc = one_step(c);
+            if (!rc) rc = online_end_step(c);
             if (rc) return rc;
-            c->state = HASHED;
+            done++;
+            continue;
         }
-        while (nsteps - done >= unroll) {
-            CK(c, cudaGraphLaunch(c->graph, c->stream));
-            done += unroll;
+        int chunk = nsteps - done;
+        if (online_active(c))
+            chunk = (int) std::min<uint64_t>((uint64_t) chunk,
+                                             c->online_period - c->steps_run % (uint64_t) c->online_period);
+        int k = 0;
+        if (chunk >= unroll) {
+            if (!c->graph || c->graph_steps != unroll || c->graph_n != c->n || c->graph_forces != c->tune.forces_mode) {
+                int rc = build_graph(c, unroll);
+                if (rc) return rc;
+                c->state = HASHED;
+            }
+            for (; chunk - k >= unroll; k += unroll) CK(c, cudaGraphLaunch(c->graph, c->stream));
+            c->n_sorted = c->n_dense = c->n_forced = c->n;
+            c->appended = false;
         }
-        c->n_sorted = c->n_dense = c->n_forced = c->n;
-        c->appended = false;
-    }
-    for (; done < nsteps; done++) {
-        int rc = one_step(c);
-        if (rc) return rc;
+        for (; k < chunk; k++) {
+            int rc = one_step(c);
+            if (rc) return rc;
+        }
+        c->steps_run += (uint64_t) chunk;
+        done += chunk;
     }
     CK(c, cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_set_online_tuning(sph_ctx *c, int32_t period)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (period != 0 && period < 3) return fail(c, SPH_ERR_ARG, "period must be 0 (off) or at least 3 steps");
+    if (period && (is_mixed(c) || (c->prm.flags & SPH_FLAG_ALL_PAIRS)))
+        return fail(c, SPH_ERR_STATE, "this context has no force variants to tune");
+    if (c->trial >= 0) return fail(c, SPH_ERR_STATE, "a tuning trial is in progress");
+    CK(c, cudaSetDevice(c->device));
+    for (auto &ev : c->on_ev)
+        if (!ev) CK(c, cudaEventCreate(&ev));
+    c->online_period = period;
     return SPH_OK;
 }
 
@@ -840,6 +924,7 @@ int sph_autotune(sph_ctx *c, int32_t reps)
     if (!rc) rc = pass_forces(c);
     if (rc) return rc;
     c->tune_pinned = true;
+    c->steps_run++;  // the step above was a real one
     tune_store(tune_key(c, c->n), bd, bf);
     return SPH_OK;
 }

@@ -28,7 +28,7 @@ SPH_FLAG_PROFILE, SPH_FLAG_RECORD_ACC, SPH_FLAG_ALL_PAIRS = 1, 2, 4
 # every symbol the header declares
 EXPORTS = (
     "sph_params_default", "sph_create", "sph_batch_create", "sph_destroy", "sph_last_error", "sph_device_name",
-    "sph_stream", "sph_set_variant", "sph_get_variant", "sph_autotune", "sph_grid_build_noalloc",
+    "sph_stream", "sph_set_variant", "sph_get_variant", "sph_autotune", "sph_set_online_tuning", "sph_grid_build_noalloc",
     "sph_upload", "sph_append", "sph_emit_fountain", "sph_set_gravity", "sph_step", "sph_pass_grid", "sph_pass_density",
     "sph_pass_forces", "sph_pass_times", "sph_get_counts", "sph_num_scenes", "sph_num_particles",
     "sph_get_resolution", "sph_download", "sph_download_f64", "sph_handoff_async", "sph_handoff_ready",
@@ -89,6 +89,7 @@ def load(path=None):
         "sph_set_variant": (i32, [vp, i32, i32]),
         "sph_get_variant": (i32, [vp, ip]),
         "sph_autotune": (i32, [vp, i32]),
+        "sph_set_online_tuning": (i32, [vp, i32]),
         "sph_grid_build_noalloc": (i32, [vp, u32, fp, f, vp, vp, vp, vp]),
         "sph_upload": (i32, [vp, vp, vp, up]),
         "sph_append": (i32, [vp, u32, vp, vp, u32]),
@@ -328,6 +329,10 @@ class SphContext:
     def autotune(self, reps=3):
         self._ck(load().sph_autotune(self.h, reps))
         return self.variant()
+
+    def set_online_tuning(self, period):
+        """Re-time the mask-driven force variants every `period` steps (0 = off)."""
+        self._ck(load().sph_set_online_tuning(self.h, period))
 
     def pass_times(self):
         ms = np.zeros(5, np.float64)

@@ -401,6 +401,42 @@ def test_splat_counts_and_depth(sphlib, tmp_path):
     ctx.close()
 
 
+def test_online_tuning_keeps_the_bits(sphlib):
+    """Online tuning switches force variants between real steps; the run is bit-identical to
+    one without it, through sph_step (graphs between trials) and through the pass calls."""
+    pos = c0_scene(sphlib, dims=(16, 16, 16))
+    runs = []
+    for mode in ("plain", "online_step", "online_passes"):
+        ctx = sphlib.SphContext(C0_BOX, pos.shape[0], gravity=G981, flags=sphlib.SPH_FLAG_RECORD_ACC)
+        ctx.upload(pos)
+        ctx.set_variant(0, 4)
+        if mode != "plain":
+            ctx.set_online_tuning(3)
+        if mode == "online_passes":
+            for _ in range(23):
+                ctx.pass_grid()
+                ctx.pass_density()
+                ctx.pass_forces()
+        else:
+            ctx.step(11)
+            ctx.step(12)
+        if mode != "plain":
+            assert ctx.variant()[1] in (4, 6, 7)
+        runs.append(ctx.download(acc=True))
+        ctx.close()
+    for r in runs[1:]:
+        for k in runs[0]:
+            assert np.array_equal(runs[0][k], r[k]), k
+    m = sphlib.SphContext(C0_BOX, 10, precision=sphlib.SPH_MIXED)
+    with pytest.raises(sphlib.SphError) as e:
+        m.set_online_tuning(10)
+    assert e.value.code == sphlib.SPH_ERR_STATE
+    with pytest.raises(sphlib.SphError) as e:
+        sphlib.SphContext(C0_BOX, 10).set_online_tuning(2)
+    assert e.value.code == sphlib.SPH_ERR_ARG
+    m.close()
+
+
 def test_device_emitter_equals_host_emitter(sphlib):
     """sph_emit_fountain generates on the device the same bits as the host generator, and a run
     fed by it equals a run fed by sph_append of the host-generated particles."""
