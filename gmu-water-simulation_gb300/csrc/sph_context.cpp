@@ -189,7 +189,7 @@ int allocate(sph_ctx *c)
     const size_t r4 = r4_bytes(c), rs = is_f64(c) ? 8 : 4;
     const bool mixed = is_mixed(c);
     const uint64_t N = c->ncap, C = c->ctot;
-    const uint64_t nb = (C + 4095) / 4096 + 1;
+    const uint64_t nb = (C + kScanTile - 1) / kScanTile + 1;
     uint64_t nobs = 0;
     for (auto &h : c->sc) nobs += h.obs.size();
     struct Item { void **p; size_t bytes; };

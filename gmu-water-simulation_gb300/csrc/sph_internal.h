@@ -122,6 +122,10 @@ struct Tune {
     int forces_mode = 3;
 };
 
+// Cells per block of the cell-count scan; the block-sum buffer holds one word per tile
+// (plus one) and is sized with this constant wherever it is allocated.
+constexpr uint32_t kScanTile = 1024;
+
 // ---- kernel launchers (sph_kernels.cu) --------------------------------------------
 template <class R>
 struct Launch {

@@ -67,9 +67,26 @@ __global__ void __launch_bounds__(256) k_ingest(Vec4<R> *__restrict__ pos_u, Vec
 // Replaces scan_local / increment_local_scans (resources/kernels/sph_grid.cl:71-121, 9-23)
 // and its sums-buffer race. The apply phase also seeds the slot cursors and zeroes the
 // counts for the next hash.
-constexpr int SCAN_THREADS = 512;
-constexpr int SCAN_PER = 8;
+// 1024-cell tiles (256 threads x 4 cells, one 16-byte access per array and thread): enough
+// blocks to fill the GPU on grids of a few hundred thousand cells.
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_PER = 4;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER;
+static_assert(SCAN_TILE == (int) kScanTile, "the scan tile and the block-sum sizing agree");
+
+// the 4 counts of a thread, 0 beyond ncells; one 16-byte load when the array is 16-byte
+// aligned (vec, decided on the host from the pointers), else 4 scalar loads
+__device__ __forceinline__ uint4 load_counts4(const uint32_t *__restrict__ count, uint32_t base, uint32_t ncells,
+                                             bool vec)
+{
+    if (vec && base + 4 <= ncells) return __ldg(reinterpret_cast<const uint4 *>(count + base));
+    if (base + 4 <= ncells) return make_uint4(count[base], count[base + 1], count[base + 2], count[base + 3]);
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (base < ncells) v.x = count[base];
+    if (base + 1 < ncells) v.y = count[base + 1];
+    if (base + 2 < ncells) v.z = count[base + 2];
+    return v;
+}
 
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &total)
 {
@@ -105,13 +122,11 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &t
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *__restrict__ count, uint32_t ncells,
-                                                              uint32_t *__restrict__ bsum)
+                                                              uint32_t *__restrict__ bsum, bool vec)
 {
     const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
-    uint32_t s = 0;
-#pragma unroll
-    for (int k = 0; k < SCAN_PER; k++)
-        if (base + k < ncells) s += count[base + k];
+    const uint4 c4 = load_counts4(count, base, ncells, vec);
+    uint32_t s = c4.x + c4.y + c4.z + c4.w;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     __shared__ uint32_t w[SCAN_THREADS / 32];
@@ -144,26 +159,24 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_top(uint32_t *__restrict_
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t *__restrict__ count, uint32_t ncells,
                                                              const uint32_t *__restrict__ bsum,
                                                              uint32_t *__restrict__ start,
-                                                             uint32_t *__restrict__ cursor)
+                                                             uint32_t *__restrict__ cursor, bool vec)
 {
     const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
-    uint32_t v[SCAN_PER];
-    uint32_t s = 0;
-#pragma unroll
-    for (int k = 0; k < SCAN_PER; k++) {
-        v[k] = base + k < ncells ? count[base + k] : 0;
-        s += v[k];
-    }
+    const uint4 c4 = load_counts4(count, base, ncells, vec);
     uint32_t total;
-    uint32_t run = block_exclusive_scan(s, total) + bsum[blockIdx.x];
-#pragma unroll
-    for (int k = 0; k < SCAN_PER; k++) {
-        if (base + k < ncells) {
-            start[base + k] = run;
-            cursor[base + k] = run;
+    const uint32_t run = block_exclusive_scan(c4.x + c4.y + c4.z + c4.w, total) + bsum[blockIdx.x];
+    const uint4 st4v = make_uint4(run, run + c4.x, run + c4.x + c4.y, run + c4.x + c4.y + c4.z);
+    if (vec && base + 4 <= ncells) {
+        *reinterpret_cast<uint4 *>(start + base) = st4v;
+        *reinterpret_cast<uint4 *>(cursor + base) = st4v;
+        *reinterpret_cast<uint4 *>(count + base) = make_uint4(0, 0, 0, 0);
+    } else {
+        const uint32_t sv[4] = {st4v.x, st4v.y, st4v.z, st4v.w};
+        for (uint32_t k = 0; k < 4 && base + k < ncells; k++) {
+            start[base + k] = sv[k];
+            cursor[base + k] = sv[k];
             count[base + k] = 0;
         }
-        run += v[k];
     }
 }
 
@@ -810,9 +823,12 @@ template <class R>
 cudaError_t Launch<R>::scan(const DevBufs &b, uint32_t ncells, cudaStream_t st)
 {
     const uint32_t nb = (ncells + SCAN_TILE - 1) / SCAN_TILE;
-    k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum);
+    // 16-byte accesses only where all three arrays allow them (a caller's start array may not)
+    const bool vec = ((reinterpret_cast<uintptr_t>(b.count) | reinterpret_cast<uintptr_t>(b.start) |
+                       reinterpret_cast<uintptr_t>(b.cursor)) & 15u) == 0;
+    k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, vec);
     k_scan_top<<<1, SCAN_THREADS, 0, st>>>(b.bsum, nb, b.start, ncells);
-    k_scan_apply<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, b.start, b.cursor);
+    k_scan_apply<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, b.start, b.cursor, vec);
     return cudaGetLastError();
 }
 

@@ -24,8 +24,7 @@ namespace {
 
 constexpr uint32_t kMaxParticles = 1u << 20;
 constexpr uint32_t kMaxCells = 1u << 20;
-constexpr uint32_t kScanTile = 4096;  // cells per scan block (the scan launcher's tile)
-constexpr uint32_t kMaxBlocks = kMaxCells / kScanTile + 1;
+constexpr uint32_t kMaxBlocks = kMaxCells / kScanTile + 1;  // scan block sums
 // counts | cursors | slot ids | scan block sums, as 32-bit words
 constexpr size_t kScratchWords = (size_t) kMaxCells + kMaxCells + kMaxParticles + kMaxBlocks;
 

@@ -29,13 +29,16 @@ def test_noalloc_grid_matches_context_grid(sphlib):
     L = sphlib.load()
     cases = [((1.0, 1.0, 0.5), sphlib.dam_break_scene((20, 20, 20), (1.0, 1.0, 0.5), seed=0)),
              ((0.45, 0.5, 0.6), sphlib.dam_break_scene((12, 9, 14), (0.45, 0.5, 0.6), seed=5) - np.float32(0.01))]
-    for box, pos in cases:  # two calls in a row, different scenes and grids
+    # calls in a row, different scenes and grids; the last writes its cell starts to an array
+    # that is 4- but not 16-byte aligned (the scan then takes its scalar path)
+    for (box, pos), offset in zip(cases + cases[:1], (0, 0, 1)):
         n = pos.shape[0]
         res = [int(np.ceil(np.float32(b) / H)) for b in box]
         ncells = res[0] * res[1] * res[2]
         xyz = torch.from_numpy(np.ascontiguousarray(pos)).cuda()
         out_cell = torch.empty(n, dtype=torch.int32, device="cuda")
-        out_start = torch.empty(ncells + 1, dtype=torch.int32, device="cuda")
+        start_buf = torch.empty(ncells + 1 + offset, dtype=torch.int32, device="cuda")
+        out_start = start_buf[offset:]
         out_order = torch.empty(n, dtype=torch.int32, device="cuda")
         boxa = (ctypes.c_float * 3)(*box)
         stream = torch.cuda.current_stream().cuda_stream
@@ -44,6 +47,7 @@ def test_noalloc_grid_matches_context_grid(sphlib):
                                       ctypes.c_void_p(out_order.data_ptr()), ctypes.c_void_p(stream))
         torch.cuda.synchronize()
         assert rc == sphlib.SPH_OK
+        assert (out_start.data_ptr() % 16 != 0) == (offset == 1)
         cell, counts, order = context_grid(sphlib, box, pos)
         start = out_start.cpu().numpy().astype(np.int64)
         assert np.array_equal(out_cell.cpu().numpy().astype(np.uint32), cell)
