@@ -70,10 +70,10 @@ def grid_cells(box):
 def alg_bytes(N, C, rs=4, forces_variant=4):
     """Compulsory DRAM bytes of each kernel of one step: every array it must touch,
     read or written once (neighbour re-reads are cache hits). rs = bytes per real.
-    Force variant 7 also has the density pass read velocities and write the packed force
+    Force variants 7-9 also have the density pass read velocities and write the packed force
     records, which the force pass then reads."""
     r4 = 4 * rs
-    rec = 3 * r4 * N if forces_variant == 7 else 0  # velocity read + 2 x r4 record written
+    rec = 3 * r4 * N if forces_variant in (7, 8, 9) else 0  # velocity read + 2 x r4 record written
     return {
         # counts read twice, starts/cursors written, counts zeroed
         "scan": 20 * C,
@@ -395,6 +395,11 @@ def main():
     ap.add_argument("--threads", type=int, default=0, help="host threads of the reference arm (0 = all)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", default=None, help="pin launch variants 'density,forces' instead of autotuning")
+    ap.add_argument("--save-state", default=None,
+                    help="write the final positions and velocities of the timed run (npz)")
+    ap.add_argument("--init-state", default=None,
+                    help="start from a state written by --save-state (the same 1M dam break, later in its "
+                         "run) instead of the initial lattice, e.g. to profile the compressed column")
     ap.add_argument("--config", default="dam1m", choices=["dam1m", "dam8k", "batch256", "fountain", "dam16m"],
                     help="dam1m is the benchmark line; the others are measured separately")
     args = ap.parse_args()
@@ -415,13 +420,18 @@ def main():
     form = {"plain": sphcuda.SPH_PLAIN_F32, "f64": sphcuda.SPH_F64, "mixed": sphcuda.SPH_MIXED}[args.form]
     rs = 8 if args.form == "f64" else 4
     pos = sphcuda.dam_break_scene(DIMS, BOX, SEED)
+    vel0 = np.zeros_like(pos)
+    if args.init_state:
+        st = np.load(args.init_state)
+        assert st["pos"].shape == pos.shape, "the state must be one of this workload"
+        pos, vel0 = np.ascontiguousarray(st["pos"], np.float32), np.ascontiguousarray(st["vel"], np.float32)
     N = pos.shape[0]
     C = grid_cells(BOX)
     dev = torch.device("cuda:0")
     torch.cuda.init()
 
     ctx = sphcuda.SphContext(BOX, N, precision=form, gravity=GRAVITY)
-    ctx.upload(pos)
+    ctx.upload(pos, vel0)
     # one untimed step picks the launch variants (all variants compute the same bits)
     if args.variant:
         ctx.set_variant(*[int(v) for v in args.variant.split(",")])
@@ -480,6 +490,8 @@ def main():
     stats = ctx.stats()
     assert stats["count"] == N and np.isfinite(stats["rho_mean"])
     resident_final = ctx.download()
+    if args.save_state:
+        np.savez(args.save_state, pos=resident_final["pos"], vel=resident_final["vel"])
     fp64_check = fp64_error(sphcuda, ctx, form, N)
 
     # bytes of each timed step by the variant it ran, against the summed event times
@@ -497,7 +509,7 @@ def main():
     # ---- end to end through the C ABI with pinned host buffers, the same state sequence:
     # from the initial upload, one untimed step, W warm-up steps, then K timed steps, each
     # uploading positions and velocities, stepping once and downloading them
-    bufs = [(torch.from_numpy(pos.copy()).pin_memory(), torch.zeros((N, 3), dtype=torch.float32).pin_memory()),
+    bufs = [(torch.from_numpy(pos.copy()).pin_memory(), torch.from_numpy(vel0.copy()).pin_memory()),
             (torch.empty((N, 3), dtype=torch.float32).pin_memory(),
              torch.empty((N, 3), dtype=torch.float32).pin_memory())]
     counts = np.array([N], np.uint32)
@@ -536,7 +548,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.form == "f64" else "f32", "data": "synthetic (seeded lattice, no dataset)",
-        "config": workload_desc({"plain": "plain FP32", "f64": "FP64", "mixed": "mixed precision"}[args.form]),
+        "config": dict(workload_desc({"plain": "plain FP32", "f64": "FP64", "mixed": "mixed precision"}[args.form]),
+                       **({"initial_state": args.init_state} if args.init_state else {})),
         "fp64_check": fp64_check,
         "roofline": {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,

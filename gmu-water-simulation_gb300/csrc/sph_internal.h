@@ -115,7 +115,8 @@ struct MixConsts {
 //               masks that the density pass then writes (density_p is ignored): 3/4 one
 //               neighbour per iteration without/with a 64-register cap, 5/6 two per
 //               iteration with/without it, 7 as 6 with each neighbour's terms read from one
-//               packed force record (two 16-byte loads from one 32-byte record)
+//               packed force record (two 16-byte loads from one 32-byte record), 8 and 9 as
+//               7 at 48 and 40 registers
 struct Tune {
     static constexpr int ALL_PAIRS = 16;  // both passes over every particle of the scene
     int density_p = 2;

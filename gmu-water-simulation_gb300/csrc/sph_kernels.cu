@@ -414,13 +414,13 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
 
 // Forces driven by the density pass's masks: only accepted neighbours are visited, in the
 // same candidate order as the scanning forms (so the sums are bit-identical).
-template <class R, int MINB>
+template <class R, int MINB, bool REC>
 __global__ void __launch_bounds__(256, MINB) k_forces_mask(
     const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
     const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
-    uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, Vec4<R> *__restrict__ pos_out,
-    Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out, uint2 *__restrict__ cid_out,
-    uint32_t *__restrict__ count)
+    uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ frec,
+    Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out,
+    uint2 *__restrict__ cid_out, uint32_t *__restrict__ count)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -459,7 +459,13 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask(
                 while (m) {
                     const uint32_t j = cb + (uint32_t) (__ffs(m) - 1);
                     m &= m - 1;
-                    if (j != i) pair_force<R>(pi, vi, qi, j, pos, vel, aux, c, fpx, fpy, fpz, fvx, fvy, fvz);
+                    if (j == i) continue;
+                    if (REC) {
+                        const Vec4<R> pj = ld4(frec + 2 * (size_t) j), vj = ld4(frec + 2 * (size_t) j + 1);
+                        pair_terms<R>(pi, vi, qi, pj, vj, pj.w, vj.w, c, fpx, fpy, fpz, fvx, fvy, fvz);
+                    } else {
+                        pair_force<R>(pi, vi, qi, j, pos, vel, aux, c, fpx, fpy, fpz, fvx, fvy, fvz);
+                    }
                 }
             }
         }
@@ -541,7 +547,9 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask2(
             }
         }
     }
-    finish_particle<R>(i, pi, vi, ai.x, sc, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
+    // the scene record again rather than kept live across the pair loop (fewer registers)
+    const SceneDev sc2 = load_scene(scenes, wbits(pi.w));
+    finish_particle<R>(i, pi, vi, ai.x, sc2, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
                        cid_out, count);
 }
 
@@ -853,7 +861,7 @@ cudaError_t Launch<R>::density(const DevBufs &b, uint32_t n, Consts<R> c, const 
         k_density_all<R><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c);
         return cudaGetLastError();
     }
-    if (t.forces_mode == 7) {  // masks and force records
+    if (t.forces_mode >= 7) {  // masks and force records
         k_density_mask<R, true><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c, b.masks,
                                                               (const Vec4<R> *) b.vel_s, (Vec4<R> *) b.frec);
         return cudaGetLastError();
@@ -885,12 +893,12 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
                                                       b.cid_u, b.count);
         break;
     case 3:
-        k_forces_mask<R, 0><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
-                                                          b.masks, po, vo, ao, b.cid_u, b.count);
+        k_forces_mask<R, 0, false><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n,
+                                                                 c, b.masks, nullptr, po, vo, ao, b.cid_u, b.count);
         break;
     case 4:
-        k_forces_mask<R, 4><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
-                                                          b.masks, po, vo, ao, b.cid_u, b.count);
+        k_forces_mask<R, 4, false><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n,
+                                                                 c, b.masks, nullptr, po, vo, ao, b.cid_u, b.count);
         break;
     case 5:
         k_forces_mask2<R, 4, false><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n,
@@ -902,6 +910,16 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
         break;
     case 7:
         k_forces_mask2<R, 0, true><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
+                                                                 b.masks, (const Vec4<R> *) b.frec, po, vo, ao,
+                                                                 b.cid_u, b.count);
+        break;
+    case 8:
+        k_forces_mask2<R, 5, true><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
+                                                                 b.masks, (const Vec4<R> *) b.frec, po, vo, ao,
+                                                                 b.cid_u, b.count);
+        break;
+    case 9:
+        k_forces_mask2<R, 6, true><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
                                                                  b.masks, (const Vec4<R> *) b.frec, po, vo, ao,
                                                                  b.cid_u, b.count);
         break;

@@ -166,7 +166,8 @@ int sph_pass_times(sph_ctx *ctx, double ms[5]);
  *            per row and the force pass visits only those (density_variant is then unused);
  *            4 trades registers for occupancy differently from 3; 5 and 6 load two accepted
  *            neighbours per iteration (with and without the register cap of 4); 7 is 6 reading each
- *            neighbour from one packed 32-byte force record written by the density pass */
+ *            neighbour from one packed 32-byte force record written by the density pass; 8 and 9
+ *            are 7 capped at 48 and 40 registers (5 and 6 blocks of 256 per SM) */
 int sph_set_variant(sph_ctx *ctx, int32_t density_variant, int32_t forces_variant);
 int sph_get_variant(const sph_ctx *ctx, int32_t out[2]);
 
@@ -180,7 +181,7 @@ int sph_autotune(sph_ctx *ctx, int32_t reps);
 /* Online tuning of the force variant for a state that changes over a run (a collapsing dam
  * break packs ~4x more neighbours per particle after a few hundred steps than at the start,
  * and the fastest variant changes with it). Every `period` steps (sph_step or the pass
- * calls), one real step runs with each of the mask-driven force variants 4, 6 and 7, timed
+ * calls), one real step runs with each of the record-reading force variants 7, 8 and 9, timed
  * with events on the context's stream (one host synchronisation per trial step), and the
  * fastest is kept until the next trial. All of them compute the same bits, so the results do
  * not depend on the choice. Applies while the current force variant is mask-driven (3..7).
