@@ -227,6 +227,15 @@ __device__ __forceinline__ void pair_terms(const Vec4<R> &pi, const Vec4<R> &vi,
                                            const Vec4<R> &vj, R qj, R invj, const Consts<R> &c, R &fpx, R &fpy,
                                            R &fpz, R &fvx, R &fvy, R &fvz);
 
+// The density pass's record of a particle: (rho, p, c_spiky p/rho^2, c_visc/rho). The last two
+// are the per-particle factors of the force terms with the kernels' constants folded in, so
+// that a pair costs two multiplications less (src/CCPUParticleSimulator.cpp:177-183).
+template <class R>
+__device__ __forceinline__ Vec4<R> aux_record(R rho, R p, const Consts<R> &c)
+{
+    return Vec4<R>{rho, p, rmul(c.c_spiky, rdiv(p, rmul(rho, rho))), rdiv(c.c_visc, rho)};
+}
+
 // Pressure and viscosity terms of one accepted neighbour (src/CCPUParticleSimulator.cpp:177-183).
 template <class R>
 __device__ __forceinline__ void pair_force(const Vec4<R> &pi, const Vec4<R> &vi, R qi, uint32_t j,
@@ -251,11 +260,12 @@ __device__ __forceinline__ void pair_terms(const Vec4<R> &pi, const Vec4<R> &vi,
     const R r2 = rfma(dz, dz, rfma(dy, dy, rmul(dx, dx)));
     const R rinv = inv_sqrt(r2);
     const R hr = rfma(-r2, rinv, c.h);
-    const R w = rmul(radd(qi, qj), rmul(rmul(rmul(c.c_spiky, hr), hr), rinv));  // (p_i/rho_i^2 + p_j/rho_j^2) grad W
+    // (p_i/rho_i^2 + p_j/rho_j^2) grad W and lap W / rho_j, the constants carried by qi, qj, invj
+    const R w = rmul(radd(qi, qj), rmul(rmul(hr, hr), rinv));
     fpx = rfma(w, dx, fpx);
     fpy = rfma(w, dy, fpy);
     fpz = rfma(w, dz, fpz);
-    const R l = rmul(rmul(c.c_visc, hr), invj);  // lap W / rho_j
+    const R l = rmul(hr, invj);
     fvx = rfma(rsub(vj.x, vi.x), l, fvx);
     fvy = rfma(rsub(vj.y, vi.y), l, fvy);
     fvz = rfma(rsub(vj.z, vi.z), l, fvz);

@@ -62,7 +62,7 @@ struct DevBufs {
     double *stats;         // per-scene FP64 reductions, 8 doubles each
     double *stats_partial; // per-scene slices of the reductions (kSplit x 6 doubles each)
     uint32_t *masks;       // accepted-neighbour bit masks of the density pass, 36 words per particle
-    void *frec;            // force records of the density pass (variant 7): (x, y, z, p/rho^2), (v, 1/rho)
+    void *frec;            // force records of the density pass (variants 7-9): (x, y, z, c_spiky p/rho^2), (v, c_visc/rho)
     // mixed-precision form only
     void *lo_s, *lo_u;     // low parts of the hi/lo positions (float4, .w unused)
     uint2 *gpos;           // gathered positions: 16-bit codes x | y << 16, z (sorted order)

@@ -242,8 +242,8 @@ __device__ __forceinline__ void for_each_row(const SceneDev &sc, const uint32_t 
 }
 
 // Density and pressure (src/CCPUParticleSimulator.cpp:93-141): rho = m * poly6 * sum (h^2-r^2)^3
-// over r^2 <= h^2, self included; p = k (rho - rho0). Also stores p / rho^2 and 1 / rho,
-// the two per-neighbour factors of the force pass.
+// over r^2 <= h^2, self included; p = k (rho - rho0). Also stores c_spiky p / rho^2 and
+// c_visc / rho, the two per-neighbour factors of the force pass (aux_record).
 template <class R>
 __global__ void __launch_bounds__(256) k_density(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
                                                  const uint32_t *__restrict__ start,
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(256) k_density(const Vec4<R> *__restrict__ pos
     });
     const R rho = rmul(rmul(acc, c.c_poly6), c.mass);
     const R p = rmul(c.k, rsub(rho, c.rho0));
-    st4(aux + i, Vec4<R>{rho, p, rdiv(p, rmul(rho, rho)), rdiv((R) 1, rho)});
+    st4(aux + i, aux_record<R>(rho, p, c));
 }
 
 // Forces, first form: one thread per sorted particle, the pair terms evaluated inside the
@@ -403,8 +403,9 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
     }
     const R rho = rmul(rmul(acc, c.c_poly6), c.mass);
     const R p = rmul(c.k, rsub(rho, c.rho0));
-    const R q = rdiv(p, rmul(rho, rho)), inv = rdiv((R) 1, rho);
-    st4(aux + i, Vec4<R>{rho, p, q, inv});
+    const Vec4<R> ar = aux_record<R>(rho, p, c);
+    const R q = ar.z, inv = ar.w;
+    st4(aux + i, ar);
     if (REC) {  // the force pass's view of this particle as a neighbour, in one 2 x 16-byte record
         const Vec4<R> vi = ld4(vel + i);
         st4(frec + 2 * (size_t) i, Vec4<R>{pi.x, pi.y, pi.z, q});
@@ -586,7 +587,7 @@ __global__ void __launch_bounds__(256) k_density_all(const Vec4<R> *__restrict__
     }
     const R rho = rmul(rmul(acc, c.c_poly6), c.mass);
     const R p = rmul(c.k, rsub(rho, c.rho0));
-    st4(aux + i, Vec4<R>{rho, p, rdiv(p, rmul(rho, rho)), rdiv((R) 1, rho)});
+    st4(aux + i, aux_record<R>(rho, p, c));
 }
 
 template <class R>
@@ -712,7 +713,7 @@ __global__ void __launch_bounds__(256) k_density_blk(const Vec4<R> *__restrict__
         if (i >= n) continue;
         const R rho = rmul(rmul(acc[p], c.c_poly6), c.mass);
         const R pr = rmul(c.k, rsub(rho, c.rho0));
-        st4(aux + i, Vec4<R>{rho, pr, rdiv(pr, rmul(rho, rho)), rdiv((R) 1, rho)});
+        st4(aux + i, aux_record<R>(rho, pr, c));
     }
 }
 
