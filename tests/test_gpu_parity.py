@@ -61,6 +61,10 @@ def scenes(sphlib, oracle_mod):
     q = c0_scene(sphlib, dims=(12, 9, 14), box=(0.45, 0.5, 0.6), seed=5)
     q[:40] -= np.float32(0.02)  # some outside the min walls: clamped cells, wall forces
     out["outside_walls"] = ((0.45, 0.5, 0.6), q, rng.normal(0, 0.2, q.shape).astype(np.float32), None)
+    # ~80 particles per cell: rows of ~250 candidates, beyond the four recorded mask words
+    # (the force kernels' fallback that tests the remaining candidates itself)
+    cl = (rng.random((1500, 3)) * 0.12 - 0.06).astype(np.float32)
+    out["dense_clump"] = ((0.5, 0.5, 0.5), cl, rng.normal(0, 0.1, cl.shape).astype(np.float32), G981)
     return out
 
 
@@ -114,7 +118,7 @@ def test_grid_cell_faces(sphlib, oracle_mod):
 
 
 # ------------------------------------------------------------------------- one step
-@pytest.mark.parametrize("name", ["ref_default_0.4", "c0_8000", "c0_8000_moving", "outside_walls"])
+@pytest.mark.parametrize("name", ["ref_default_0.4", "c0_8000", "c0_8000_moving", "outside_walls", "dense_clump"])
 def test_one_step_plain_vs_oracle(sphlib, oracle_mod, name):
     box, pos, vel, g = scenes(sphlib, oracle_mod)[name]
     got = gpu_run(sphlib, box, pos, vel, gravity=g)
@@ -498,6 +502,34 @@ def test_reference_shaped_simulator(sphlib, oracle_mod, tmp_path):
     assert open(d).read().splitlines()[1].startswith("Grid;")
 
 
+def test_empty_and_single_particle_scenes(sphlib):
+    """A batch holding an empty scene, a lone particle and a small dam break: the lone particle
+    has the self density m poly6(0) and falls with gravity exactly, the dam break equals a
+    run of its own, and the empty scene stays empty."""
+    boxes = [(0.3, 0.3, 0.3), (0.5, 0.5, 0.5), C0_BOX]
+    dam = c0_scene(sphlib, dims=(8, 8, 8))
+    lone = np.zeros((1, 3), np.float32)
+    ctx = sphlib.SphContext(boxes, [10, 1, dam.shape[0]], gravity=G981, flags=sphlib.SPH_FLAG_RECORD_ACC)
+    ctx.upload(np.concatenate([lone, dam]), None, [0, 1, dam.shape[0]])
+    ctx.step(3)
+    d = ctx.download(acc=True)
+    assert list(ctx.counts()) == [0, 1, dam.shape[0]]
+    h = np.float32(0.0457)
+    self_rho = np.float32(0.02) * np.float32(315.0 / (64.0 * np.pi * float(h) ** 9)) * np.float32(h * h) ** 3
+    assert abs(d["rho"][0] - self_rho) / self_rho < 1e-6
+    assert np.allclose(d["acc"][0], np.float32(G981), rtol=1e-6, atol=0)
+    st = ctx.stats(0)
+    assert st["count"] == 0 and st["mass"] == 0.0
+    ctx.close()
+    one = sphlib.SphContext(C0_BOX, dam.shape[0], gravity=G981, flags=sphlib.SPH_FLAG_RECORD_ACC)
+    one.upload(dam)
+    one.step(3)
+    e = one.download(acc=True)
+    one.close()
+    for k in e:
+        assert np.array_equal(d[k][1:], e[k]), k
+
+
 def test_errors_are_status_codes(sphlib):
     ctx = sphlib.SphContext((0.4, 0.4, 0.4), 10)
     with pytest.raises(sphlib.SphError) as e:
@@ -584,7 +616,8 @@ def test_full_size_1m_properties(sphlib):
 def test_variants_bit_identical(sphlib, oracle_mod):
     """Every launch variant of the two neighbour passes computes the same bits."""
     for box, pos, vel, g in [scenes(sphlib, oracle_mod)["c0_8000_moving"],
-                             scenes(sphlib, oracle_mod)["outside_walls"]]:
+                             scenes(sphlib, oracle_mod)["outside_walls"],
+                             scenes(sphlib, oracle_mod)["dense_clump"]]:
         base = None
         for dv, fv in [(d, f) for d in (0, 1, 2, 4) for f in (0, 1, 2)] + [(0, 3), (0, 4), (0, 5), (0, 6), (0, 7), (0, 8), (0, 9)]:
             if True:
