@@ -168,6 +168,20 @@ int upload_scenes(sph_ctx *c)
     return SPH_OK;
 }
 
+// Device-accessible view of a pinned (page-locked) host array, or nullptr for other memory.
+// Kernels then read or write the caller's array over the host link directly: the transfer
+// and the ingest (or the id-ordered gather) become one pass.
+void *pinned_view(const void *p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // not an error of the context: the copy path is taken
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int upload_scene_off(sph_ctx *c)
 {
     c->scene_off_host.assign(c->sc.size() + 1, 0);
@@ -216,6 +230,7 @@ int allocate(sph_ctx *c)
         {(void **) &b.stats_partial, 6 * 8 * 64 * c->sc.size()},
         {(void **) &b.masks, 4 * 36 * N},
         {(void **) &b.frec, mixed ? 0 : 2 * r4 * N},
+        {(void **) &b.inv, 4 * N},
     };
     size_t total = 0;
     for (auto &it : items) total += (it.bytes + 255) & ~size_t(255);
@@ -626,14 +641,21 @@ int sph_upload(sph_ctx *c, const float *xyz, const float *vel, const uint32_t *c
         CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
         if (total) {
             if (is_mixed(c)) CK(c, cudaMemsetAsync(c->b.lo_u, 0, 16 * total, c->stream));
-            CK(c, cudaMemcpyAsync(c->b.st_xyz, xyz, 12 * total, cudaMemcpyHostToDevice, c->stream));
-            if (vel) CK(c, cudaMemcpyAsync(c->b.st_vel, vel, 12 * total, cudaMemcpyHostToDevice, c->stream));
+            // pinned caller arrays are read by the ingest kernel itself; others go through staging
+            const float *sx = (const float *) pinned_view(xyz);
+            const float *sv = vel ? (const float *) pinned_view(vel) : nullptr;
+            if (!sx || (vel && !sv)) {
+                CK(c, cudaMemcpyAsync(c->b.st_xyz, xyz, 12 * total, cudaMemcpyHostToDevice, c->stream));
+                if (vel) CK(c, cudaMemcpyAsync(c->b.st_vel, vel, 12 * total, cudaMemcpyHostToDevice, c->stream));
+                sx = c->b.st_xyz;
+                sv = vel ? c->b.st_vel : nullptr;
+            }
             if (is_f64(c))
-                CK(c, Launch<double>::ingest(c->b, c->b.st_xyz, vel ? c->b.st_vel : nullptr, 0, c->n, -1, 0,
-                                             (uint32_t) c->sc.size(), make_consts<double>(c->prm), c->stream));
+                CK(c, Launch<double>::ingest(c->b, sx, sv, 0, c->n, -1, 0, (uint32_t) c->sc.size(),
+                                             make_consts<double>(c->prm), c->stream));
             else
-                CK(c, Launch<float>::ingest(c->b, c->b.st_xyz, vel ? c->b.st_vel : nullptr, 0, c->n, -1, 0,
-                                            (uint32_t) c->sc.size(), make_consts<float>(c->prm), c->stream));
+                CK(c, Launch<float>::ingest(c->b, sx, sv, 0, c->n, -1, 0, (uint32_t) c->sc.size(),
+                                            make_consts<float>(c->prm), c->stream));
         }
         int dv, fv;
         if (!c->tune_pinned && tune_lookup(tune_key(c, total), dv, fv)) {
@@ -970,6 +992,17 @@ static int download_impl(sph_ctx *c, void *xyz, void *vel, void *rho, void *p, v
     if (rc) return rc;
     const int layout_sorted = (c->state == SORTED || c->state == DENSE) ? 1 : 0;
     const int aux_sorted = c->state == DENSE ? 1 : 0;
+    // plain FP32 positions and velocities into pinned arrays: written there by one gather
+    if (!f64 && !is_f64(c) && !is_mixed(c) && !rho && !p && !acc && (xyz || vel)) {
+        float *vx = xyz ? (float *) pinned_view(xyz) : nullptr;
+        float *vv = vel ? (float *) pinned_view(vel) : nullptr;
+        const bool aligned = ((reinterpret_cast<uintptr_t>(vx) | reinterpret_cast<uintptr_t>(vv)) & 15u) == 0;
+        if ((!xyz || vx) && (!vel || vv) && aligned) {
+            CK(c, launch_gather_host<float>(c->b, c->n, layout_sorted, vx, vv, c->stream));
+            CK(c, cudaStreamSynchronize(c->stream));
+            return SPH_OK;
+        }
+    }
     const size_t rs = f64 ? 8 : 4;
     const uint32_t n = c->n;
     DevBufs &b = c->b;

@@ -96,6 +96,73 @@ cudaError_t launch_splat(const DevBufs &b, uint32_t n, int layout_sorted, uint32
     return cudaGetLastError();
 }
 
+// Download straight into the caller's pinned host arrays: the id-ordered index of every
+// particle first (a scatter within device memory), then one gather that writes the float3
+// arrays in id order, so that the writes over the host link are contiguous.
+template <class R>
+__global__ void __launch_bounds__(256) k_id_index(const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel,
+                                                  const uint32_t *__restrict__ scene_off, uint32_t n,
+                                                  uint32_t *__restrict__ inv)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = __ldg(scene_off + wbits(ldc4(pos + i).w)) + wbits(ldc4(vel + i).w);
+    if (o < n) inv[o] = i;
+}
+
+// 256 particles per block: the block's 3 x 256 floats of each array are assembled in shared
+// memory and written out as 16-byte stores (the arrays are 16-byte aligned: the caller checks),
+// so that the host link sees whole contiguous lines
+template <class R>
+__global__ void __launch_bounds__(256) k_gather_host(const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel,
+                                                     const uint32_t *__restrict__ inv, uint32_t n,
+                                                     float *__restrict__ xyz, float *__restrict__ v)
+{
+    __shared__ __align__(16) float buf[2][3 * 256];
+    const uint32_t o0 = blockIdx.x * 256, o = o0 + threadIdx.x;
+    const uint32_t cnt = min(256u, n - o0);  // particles of this block
+    if (o < n) {
+        const uint32_t i = __ldg(inv + o);
+        if (xyz) {
+            const Vec4<R> pp = ldc4(pos + i);
+            buf[0][3 * threadIdx.x] = (float) pp.x;
+            buf[0][3 * threadIdx.x + 1] = (float) pp.y;
+            buf[0][3 * threadIdx.x + 2] = (float) pp.z;
+        }
+        if (v) {
+            const Vec4<R> vv = ldc4(vel + i);
+            buf[1][3 * threadIdx.x] = (float) vv.x;
+            buf[1][3 * threadIdx.x + 1] = (float) vv.y;
+            buf[1][3 * threadIdx.x + 2] = (float) vv.z;
+        }
+    }
+    __syncthreads();
+    const uint32_t nf = 3 * cnt;  // floats of this block per array
+    for (int a = 0; a < 2; a++) {
+        float *dst = a == 0 ? xyz : v;
+        if (!dst) continue;
+        float *out = dst + 3 * (size_t) o0;  // 16-byte aligned: o0 is a multiple of 256
+        for (uint32_t k = threadIdx.x; 4 * k < nf; k += 256) {
+            if (4 * k + 4 <= nf)
+                *reinterpret_cast<float4 *>(out + 4 * k) = *reinterpret_cast<const float4 *>(&buf[a][4 * k]);
+            else
+                for (uint32_t e = 4 * k; e < nf; e++) out[e] = buf[a][e];
+        }
+    }
+}
+
+template <class R>
+cudaError_t launch_gather_host(const DevBufs &b, uint32_t n, int layout_sorted, float *xyz, float *v, cudaStream_t st)
+{
+    if (!n) return cudaSuccess;
+    const Vec4<R> *pos = (const Vec4<R> *) (layout_sorted ? b.pos_s : b.pos_u);
+    const Vec4<R> *vel = (const Vec4<R> *) (layout_sorted ? b.vel_s : b.vel_u);
+    k_id_index<R><<<(n + 255) / 256, 256, 0, st>>>(pos, vel, b.scene_off, n, b.inv);
+    k_gather_host<R><<<(n + 255) / 256, 256, 0, st>>>(pos, vel, b.inv, n, xyz, v);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_gather_host<float>(const DevBufs &, uint32_t, int, float *, float *, cudaStream_t);
 template cudaError_t launch_handoff<float>(const DevBufs &, uint32_t, int, float *, float *, cudaStream_t);
 template cudaError_t launch_handoff<double>(const DevBufs &, uint32_t, int, float *, float *, cudaStream_t);
 template cudaError_t launch_splat<float>(const DevBufs &, uint32_t, int, uint32_t, int, float, float, float, float,

@@ -63,6 +63,7 @@ struct DevBufs {
     double *stats_partial; // per-scene slices of the reductions (kSplit x 6 doubles each)
     uint32_t *masks;       // accepted-neighbour bit masks of the density pass, 36 words per particle
     void *frec;            // force records of the density pass (variants 7-9): (x, y, z, c_spiky p/rho^2), (v, c_visc/rho)
+    uint32_t *inv;         // layout index of each particle in id order (downloads into pinned host memory)
     // mixed-precision form only
     void *lo_s, *lo_u;     // low parts of the hi/lo positions (float4, .w unused)
     uint2 *gpos;           // gathered positions: 16-bit codes x | y << 16, z (sorted order)
@@ -157,6 +158,11 @@ cudaError_t launch_emit_fountain(uint64_t seed, uint32_t step, uint32_t n, const
 // id-ordered float3 positions (and velocities if v) of the first n particles (sph_handoff.cu)
 template <class R>
 cudaError_t launch_handoff(const DevBufs &b, uint32_t n, int layout_sorted, float *xyz, float *v, cudaStream_t st);
+
+// id-ordered float3 positions and/or velocities written straight into pinned host arrays
+// (device-accessible views), through b.inv (sph_handoff.cu)
+template <class R>
+cudaError_t launch_gather_host(const DevBufs &b, uint32_t n, int layout_sorted, float *xyz, float *v, cudaStream_t st);
 
 // orthographic point splat of one scene into per-pixel counts and nearest depth (sph_handoff.cu)
 template <class R>

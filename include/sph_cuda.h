@@ -116,7 +116,11 @@ void *sph_stream(const sph_ctx *ctx);
 /* Replaces every scene's particles: counts[s] particles for scene s, concatenated
  * scene-major; vel may be NULL (zero). Ids restart at 0 in each scene. Mirrors
  * setupScene's addParticle loop (src/CBaseParticleSimulator.cpp:38-74) followed by the
- * first H2D copy of CGPUParticleSimulator::updateGrid (src/CGPUParticleSimulator.cpp:59). */
+ * first H2D copy of CGPUParticleSimulator::updateGrid (src/CGPUParticleSimulator.cpp:59).
+ * Pinned (page-locked) arrays are read by the ingest kernel over the host link, without a
+ * staging copy; the call then returns before they are read, so keep them unchanged until
+ * the next synchronising call (a download, or sph_stream's work done). Other host memory is
+ * copied before the call returns. */
 int sph_upload(sph_ctx *ctx, const float *xyz, const float *vel, const uint32_t *counts);
 
 /* Appends n particles to one scene (emitters, e.g. the FOUNTAIN scenario's
@@ -199,7 +203,9 @@ int sph_get_resolution(const sph_ctx *ctx, uint32_t scene, int32_t res[3]);
 /* State after the last call, scene-major and in id order. Any pointer may be NULL.
  * rho / p are the densities and pressures of the last density pass; acc needs
  * SPH_FLAG_RECORD_ACC. Replaces the readback of CGPUBaseParticleSimulator::integrate
- * (src/CGPUBaseParticleSimulator.cpp:84-91). */
+ * (src/CGPUBaseParticleSimulator.cpp:84-91). Plain FP32 positions and velocities alone,
+ * into 16-byte-aligned pinned arrays, are written there by one gather kernel over the host
+ * link (no staging copy); the call returns when the data is in place either way. */
 int sph_download(sph_ctx *ctx, float *xyz, float *vel, float *rho, float *p, float *acc);
 /* Same in double, for SPH_F64 contexts. */
 int sph_download_f64(sph_ctx *ctx, double *xyz, double *vel, double *rho, double *p, double *acc);

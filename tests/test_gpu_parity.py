@@ -441,6 +441,49 @@ def test_online_tuning_keeps_the_bits(sphlib):
     m.close()
 
 
+def test_pinned_transfers_equal_staged_transfers(sphlib):
+    """Uploads from and downloads into pinned host arrays go straight through kernels (no
+    staging copy); they give the same bits as pageable arrays, for a batch, after a whole step
+    and between passes (the two state layouts)."""
+    import torch
+
+    dims, boxes = sphlib.batch_plan(3, seed=9, nmin=500, nmax=3000)
+    parts = [sphlib.dam_break_scene(tuple(int(x) for x in d), tuple(float(x) for x in b), seed=s)
+             for s, (d, b) in enumerate(zip(dims, boxes))]
+    counts = [q.shape[0] for q in parts]
+    pos = np.concatenate(parts)
+    vel = np.random.default_rng(3).normal(0, 0.1, pos.shape).astype(np.float32)
+    n = pos.shape[0]
+    px, pv = torch.from_numpy(pos.copy()).pin_memory(), torch.from_numpy(vel.copy()).pin_memory()
+    runs = []
+    for pinned in (False, True):
+        ctx = sphlib.SphContext(boxes, counts, gravity=G981)
+        if pinned:
+            ctx.upload_raw(px.data_ptr(), pv.data_ptr(), counts)
+        else:
+            ctx.upload(pos, vel, counts)
+        ctx.step(4)
+        got = []
+        for mid_step in (False, True):
+            if mid_step:
+                ctx.pass_grid()  # sorted layout
+            if pinned:
+                ox, ov = torch.empty((n, 3)).pin_memory(), torch.empty((n, 3)).pin_memory()
+                ctx.download_raw(ox.data_ptr(), ov.data_ptr())
+                got.append((ox.numpy().copy(), ov.numpy().copy()))
+                # a pinned array that is not 16-byte aligned takes the staging path: same bits
+                big = torch.empty(3 * n + 1).pin_memory()
+                ctx.download_raw(big.data_ptr() + 4, ov.data_ptr())
+                assert np.array_equal(big.numpy()[1:].reshape(n, 3), got[-1][0])
+            else:
+                d = ctx.download()
+                got.append((d["pos"], d["vel"]))
+        runs.append(got)
+        ctx.close()
+    for (a, b) in zip(runs[0], runs[1]):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
 def test_device_emitter_equals_host_emitter(sphlib):
     """sph_emit_fountain generates on the device the same bits as the host generator, and a run
     fed by it equals a run fed by sph_append of the host-generated particles."""
