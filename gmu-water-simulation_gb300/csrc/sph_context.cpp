@@ -198,7 +198,15 @@ void drop_graph(sph_ctx *c)
     c->graph_steps = 0;
 }
 
-int allocate(sph_ctx *c)
+struct PoolItem {
+    void **p;
+    size_t bytes;
+};
+
+// The sub-arrays of a context's single device allocation (256-byte aligned); returns the
+// total size. Needs only the configuration (no CUDA call), so a create can be refused before
+// any device work and sph_memory_required can answer on the host.
+size_t pool_layout(sph_ctx *c, std::vector<PoolItem> &items)
 {
     const size_t r4 = r4_bytes(c), rs = is_f64(c) ? 8 : 4;
     const bool mixed = is_mixed(c);
@@ -206,10 +214,9 @@ int allocate(sph_ctx *c)
     const uint64_t nb = (C + kScanTile - 1) / kScanTile + 1;
     uint64_t nobs = 0;
     for (auto &h : c->sc) nobs += h.obs.size();
-    struct Item { void **p; size_t bytes; };
     DevBufs &b = c->b;
     const bool rec = (c->prm.flags & SPH_FLAG_RECORD_ACC) != 0;
-    std::vector<Item> items = {
+    items = {
         {&b.pos_s, r4 * N}, {&b.vel_s, r4 * N}, {&b.pos_u, r4 * N}, {&b.vel_u, r4 * N}, {&b.aux, r4 * N},
         {&b.acc, rec ? r4 * N : 0},
         {(void **) &b.cid_u, 8 * N}, {(void **) &b.tmp, 4 * N},
@@ -234,6 +241,24 @@ int allocate(sph_ctx *c)
     };
     size_t total = 0;
     for (auto &it : items) total += (it.bytes + 255) & ~size_t(255);
+    return total;
+}
+
+// SPH_DEVICE_MEMORY_LIMIT (bytes): an optional cap on a context's device allocation, e.g. to
+// share a GPU with other work; 0 or unset = no cap
+uint64_t memory_limit()
+{
+    const char *v = std::getenv("SPH_DEVICE_MEMORY_LIMIT");
+    return v ? std::strtoull(v, nullptr, 10) : 0;
+}
+
+int allocate(sph_ctx *c)
+{
+    std::vector<PoolItem> items;
+    const size_t total = pool_layout(c, items);
+    DevBufs &b = c->b;
+    const uint64_t N = c->ncap, C = c->ctot;
+    const size_t r4 = r4_bytes(c);
     cudaError_t e = cudaMalloc(&c->pool, total);
     if (e != cudaSuccess) {
         c->pool = nullptr;
@@ -254,10 +279,10 @@ int allocate(sph_ctx *c)
 // the all-pairs form is O(n^2) per scene: a check for small scenes, not a production path
 constexpr uint32_t kAllPairsMax = 131072;
 
-int create_common(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *scenes, sph_ctx **out)
+// Validates the parameters and scenes and fills the host side of a context (scenes, cells,
+// capacity, tune); no CUDA call. Errors are reported as create errors (sph_last_error(NULL)).
+int parse_config(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *scenes, sph_ctx *c)
 {
-    if (!out) return fail(nullptr, SPH_ERR_ARG, "out is NULL");
-    *out = nullptr;
     if (!p || !scenes || n_scenes == 0) return fail(nullptr, SPH_ERR_ARG, "params/scenes missing or n_scenes == 0");
     if (p->struct_size != sizeof(sph_params)) return fail(nullptr, SPH_ERR_ARG, "sph_params.struct_size mismatch");
     if (!(p->h > 0) || !(p->dt > 0) || !(p->mass > 0)) return fail(nullptr, SPH_ERR_ARG, "h, dt and mass must be > 0");
@@ -270,8 +295,6 @@ int create_common(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *
         if (scenes[s].max_particles > kAllPairsMax)
             return fail(nullptr, SPH_ERR_CAPACITY, "scene " + std::to_string(s) + ": the all-pairs form takes at most " +
                                                        std::to_string(kAllPairsMax) + " particles per scene");
-    sph_ctx *c = new (std::nothrow) sph_ctx();
-    if (!c) return fail(nullptr, SPH_ERR_NOMEM, "host allocation failed");
     c->prm = *p;
     if (all_pairs) {  // both passes over every particle of the scene; no variants to choose
         c->tune.density_p = Tune::ALL_PAIRS;
@@ -284,10 +307,8 @@ int create_common(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *
         const sph_scene_desc &d = scenes[s];
         SceneHost h{};
         for (int a = 0; a < 3; a++) {
-            if (!(d.box[a] > 0) || !std::isfinite(d.box[a])) {
-                delete c;
+            if (!(d.box[a] > 0) || !std::isfinite(d.box[a]))
                 return fail(nullptr, SPH_ERR_ARG, "scene " + std::to_string(s) + ": box extents must be finite and > 0");
-            }
             h.box[a] = d.box[a];
             h.res[a] = (int32_t) std::ceil(d.box[a] / p->h);  // float division, then ceil
             h.gravity[a] = p->gravity[a];
@@ -297,10 +318,8 @@ int create_common(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *
         h.ncells = (uint32_t) nc;
         h.cap = d.max_particles;
         h.count = 0;
-        if (d.n_obstacles && !d.obstacles) {
-            delete c;
+        if (d.n_obstacles && !d.obstacles)
             return fail(nullptr, SPH_ERR_ARG, "scene " + std::to_string(s) + ": obstacles pointer is NULL");
-        }
         for (uint32_t o = 0; o < d.n_obstacles; o++) {
             ObstacleDev ob{};
             for (int a = 0; a < 3; a++) {
@@ -313,12 +332,35 @@ int create_common(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *
         ncap += d.max_particles;
         c->sc.push_back(h);
     }
-    if (ctot >= (1ull << 31) || ncap >= (1ull << 31) || ncap == 0) {
-        delete c;
+    if (ctot >= (1ull << 31) || ncap >= (1ull << 31) || ncap == 0)
         return fail(nullptr, SPH_ERR_ARG, "total cells and particle capacity must be in [1, 2^31)");
-    }
     c->ctot = ctot;
     c->ncap = ncap;
+    return SPH_OK;
+}
+
+int create_common(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *scenes, sph_ctx **out)
+{
+    if (!out) return fail(nullptr, SPH_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    sph_ctx *c = new (std::nothrow) sph_ctx();
+    if (!c) return fail(nullptr, SPH_ERR_NOMEM, "host allocation failed");
+    int prc = parse_config(p, n_scenes, scenes, c);
+    if (prc) {
+        delete c;
+        return prc;
+    }
+    {
+        std::vector<PoolItem> items;
+        const uint64_t need = pool_layout(c, items), limit = memory_limit();
+        c->b = DevBufs{};
+        if (limit && need > limit) {
+            delete c;
+            return fail(nullptr, SPH_ERR_NOMEM, "the context needs " + std::to_string(need) +
+                                                    " bytes of device memory, above SPH_DEVICE_MEMORY_LIMIT (" +
+                                                    std::to_string(limit) + ")");
+        }
+    }
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -591,6 +633,21 @@ int sph_batch_create(const sph_params *p, uint32_t n_scenes, const sph_scene_des
         return create_common(p, n_scenes, scenes, out);
     } catch (...) {
         return fail(nullptr, SPH_ERR_NOMEM, "host exception in sph_batch_create");
+    }
+}
+
+int sph_memory_required(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *scenes, uint64_t *bytes)
+{
+    if (!bytes) return fail(nullptr, SPH_ERR_ARG, "bytes is NULL");
+    try {
+        sph_ctx c;  // host side only: no device, no stream
+        const int rc = parse_config(p, n_scenes, scenes, &c);
+        if (rc) return rc;
+        std::vector<PoolItem> items;
+        *bytes = pool_layout(&c, items);
+        return SPH_OK;
+    } catch (...) {
+        return fail(nullptr, SPH_ERR_NOMEM, "host exception in sph_memory_required");
     }
 }
 

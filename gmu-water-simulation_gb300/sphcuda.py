@@ -27,7 +27,7 @@ SPH_FLAG_PROFILE, SPH_FLAG_RECORD_ACC, SPH_FLAG_ALL_PAIRS = 1, 2, 4
 
 # every symbol the header declares
 EXPORTS = (
-    "sph_params_default", "sph_create", "sph_batch_create", "sph_destroy", "sph_last_error", "sph_device_name",
+    "sph_params_default", "sph_create", "sph_batch_create", "sph_memory_required", "sph_destroy", "sph_last_error", "sph_device_name",
     "sph_stream", "sph_set_variant", "sph_get_variant", "sph_autotune", "sph_set_online_tuning", "sph_grid_build_noalloc",
     "sph_upload", "sph_append", "sph_emit_fountain", "sph_set_gravity", "sph_step", "sph_pass_grid", "sph_pass_density",
     "sph_pass_forces", "sph_pass_times", "sph_get_counts", "sph_num_scenes", "sph_num_particles",
@@ -82,6 +82,8 @@ def load(path=None):
         "sph_create": (i32, [ctypes.POINTER(sph_params), fp, u32, ctypes.POINTER(vp)]),
         "sph_batch_create": (i32, [ctypes.POINTER(sph_params), u32, ctypes.POINTER(sph_scene_desc),
                                    ctypes.POINTER(vp)]),
+        "sph_memory_required": (i32, [ctypes.POINTER(sph_params), u32, ctypes.POINTER(sph_scene_desc),
+                                      ctypes.POINTER(ctypes.c_uint64)]),
         "sph_destroy": (None, [vp]),
         "sph_last_error": (ctypes.c_char_p, [vp]),
         "sph_device_name": (ctypes.c_char_p, [vp]),

@@ -100,6 +100,13 @@ int sph_create(const sph_params *p, const float box[3], uint32_t max_particles, 
  * per pass over all scenes). */
 int sph_batch_create(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *scenes, sph_ctx **out);
 
+/* Device memory a context with these parameters and scenes would allocate (one pool), without
+ * creating it or touching a GPU. The optional handoff buffers (24 bytes per particle of
+ * capacity, allocated by the first sph_handoff_async or sph_export_positions) are not
+ * included. Creating a context fails with SPH_ERR_NOMEM, before any device work, when this
+ * exceeds the environment variable SPH_DEVICE_MEMORY_LIMIT (bytes; unset or 0 = no limit). */
+int sph_memory_required(const sph_params *params, uint32_t n_scenes, const sph_scene_desc *scenes, uint64_t *bytes);
+
 void sph_destroy(sph_ctx *ctx);
 
 /* Last error message of ctx (or of the last failed create when ctx is NULL). */

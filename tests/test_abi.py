@@ -96,3 +96,31 @@ def test_create_without_gpu_reports_cuda_error(sphlib):
     assert rc == sphlib.SPH_ERR_CUDA and msg
     with pytest.raises(sphlib.SphError):
         sphlib.SphContext([1.0, 1.0, 1.0], 10)
+
+
+def test_memory_required_and_limit(sphlib, monkeypatch):
+    """The device memory of a configuration is known on the host, and a context above
+    SPH_DEVICE_MEMORY_LIMIT is refused with SPH_ERR_NOMEM before any device work."""
+    L = sphlib.load()
+
+    def required(cap, box=(5.0, 5.0, 2.5), **kw):
+        p = sphlib.default_params(**kw)
+        d = (sphlib.sph_scene_desc * 1)()
+        for a in range(3):
+            d[0].box[a] = box[a]
+        d[0].max_particles = cap
+        out = ctypes.c_uint64()
+        rc = L.sph_memory_required(ctypes.byref(p), 1, d, ctypes.byref(out))
+        return rc, out.value
+
+    rc, b1 = required(1_000_000)
+    assert rc == sphlib.SPH_OK and 250e6 < b1 < 450e6  # ~330 B per particle + ~50 B per cell
+    rc, b2 = required(2_000_000)
+    assert rc == sphlib.SPH_OK and 1.8 < b2 / b1 < 2.0
+    rc, b3 = required(1_000_000, precision=sphlib.SPH_F64)
+    assert rc == sphlib.SPH_OK and b3 > b1
+    rc, _ = required(0)
+    assert rc == sphlib.SPH_ERR_ARG
+    monkeypatch.setenv("SPH_DEVICE_MEMORY_LIMIT", str(b1 - 1))
+    rc, h, msg = _create(sphlib, box=(5.0, 5.0, 2.5), cap=1_000_000)
+    assert rc == sphlib.SPH_ERR_NOMEM and "SPH_DEVICE_MEMORY_LIMIT" in msg and not h.value

@@ -573,6 +573,37 @@ def test_empty_and_single_particle_scenes(sphlib):
         assert np.array_equal(d[k][1:], e[k]), k
 
 
+@pytest.mark.parametrize("prec", ["plain", "f64"])
+def test_nan_particle_is_isolated(sphlib, prec):
+    """A particle with a NaN coordinate in the host input fails every neighbour test (h^2 - r^2
+    is NaN, not > 0): every other particle's state is bit-identical to a run without it, and
+    the run does not fail. The NaN particle itself stays non-finite."""
+    P = {"plain": sphlib.SPH_PLAIN_F32, "f64": sphlib.SPH_F64}[prec]
+    pos = c0_scene(sphlib, dims=(12, 12, 12))
+    vel = np.random.default_rng(6).normal(0, 0.2, pos.shape).astype(np.float32)
+    n = pos.shape[0]
+    bad = np.concatenate([pos, np.float32([[np.nan, -0.3, 0.05]])])
+    badv = np.concatenate([vel, np.zeros((1, 3), np.float32)])
+    out = []
+    for p_, v_ in ((pos, vel), (bad, badv)):
+        ctx = sphlib.SphContext(C0_BOX, p_.shape[0], precision=P, gravity=G981)
+        ctx.upload(p_, v_)
+        ctx.step(5)
+        if prec == "f64":
+            import ctypes
+            x = np.zeros((p_.shape[0], 3)); v = np.zeros((p_.shape[0], 3)); r = np.zeros(p_.shape[0])
+            sphlib.load().sph_download_f64(ctx.h, ctypes.c_void_p(x.ctypes.data), ctypes.c_void_p(v.ctypes.data),
+                                           ctypes.c_void_p(r.ctypes.data), None, None)
+            out.append({"pos": x, "vel": v, "rho": r})
+        else:
+            out.append(ctx.download())
+        ctx.close()
+    a, b = out
+    for k in ("pos", "vel", "rho"):
+        assert np.array_equal(a[k], b[k][:n]), k
+    assert not np.all(np.isfinite(b["pos"][n]))
+
+
 def test_errors_are_status_codes(sphlib):
     ctx = sphlib.SphContext((0.4, 0.4, 0.4), 10)
     with pytest.raises(sphlib.SphError) as e:
