@@ -70,10 +70,10 @@ def grid_cells(box):
 def alg_bytes(N, C, rs=4, forces_variant=4):
     """Compulsory DRAM bytes of each kernel of one step: every array it must touch,
     read or written once (neighbour re-reads are cache hits). rs = bytes per real.
-    Force variants 7-9 also have the density pass read velocities and write the packed force
+    Force variants 7 and up also have the density pass read velocities and write the packed force
     records, which the force pass then reads."""
     r4 = 4 * rs
-    rec = 3 * r4 * N if forces_variant in (7, 8, 9) else 0  # velocity read + 2 x r4 record written
+    rec = 3 * r4 * N if forces_variant >= 7 else 0  # velocity read + 2 x r4 record written
     return {
         # counts read twice, starts/cursors written, counts zeroed
         "scan": 20 * C,
