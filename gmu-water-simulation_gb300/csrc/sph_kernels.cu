@@ -192,8 +192,15 @@ __global__ void __launch_bounds__(256) k_slot(const uint2 *__restrict__ cid_u, u
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 cd = cid_u[i];
-    const uint32_t p = atomicAdd(cursor + cd.x, 1u);
-    tmp[p] = cd.y;
+    // consecutive particles mostly share a cell: one atomic per cell and warp, each lane taking
+    // its rank among the warp's lanes of that cell (the slot order is arbitrary anyway)
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned peers = __match_any_sync(__activemask(), cd.x);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if ((int) lane == leader) base = atomicAdd(cursor + cd.x, (uint32_t) __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    tmp[base + (uint32_t) __popc(peers & ((1u << lane) - 1u))] = cd.y;
 }
 
 template <class R>
