@@ -63,7 +63,8 @@ __global__ void __launch_bounds__(256) k_ingest(Vec4<R> *__restrict__ pos_u, Vec
 }
 
 // ------------------------------------------------------------------------------------
-// Exclusive scan of the per-cell counts into cell starts (reduce, top-level scan, apply).
+// Exclusive scan of the per-cell counts into cell starts (per-tile sums, then per tile the
+// offset from the earlier sums and the scan of the tile).
 // Replaces scan_local / increment_local_scans (resources/kernels/sph_grid.cl:71-121, 9-23)
 // and its sums-buffer race. The apply phase also seeds the slot cursors and zeroes the
 // counts for the next hash.
@@ -140,22 +141,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *__
     }
 }
 
-// one block: exclusive scan of the block sums (any count, in chunks), total -> start[ncells]
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_top(uint32_t *__restrict__ bsum, uint32_t nb,
-                                                           uint32_t *__restrict__ start, uint32_t ncells)
-{
-    uint32_t carry = 0;
-    for (uint32_t base = 0; base < nb; base += SCAN_THREADS) {
-        const uint32_t i = base + threadIdx.x;
-        const uint32_t v = i < nb ? bsum[i] : 0;
-        uint32_t total;
-        const uint32_t e = block_exclusive_scan(v, total);
-        if (i < nb) bsum[i] = carry + e;
-        carry += total;
-    }
-    if (threadIdx.x == 0) start[ncells] = carry;
-}
-
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t *__restrict__ count, uint32_t ncells,
                                                              const uint32_t *__restrict__ bsum,
                                                              uint32_t *__restrict__ start,
@@ -163,8 +148,20 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t *__restric
 {
     const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
     const uint4 c4 = load_counts4(count, base, ncells, vec);
+    // this tile's offset: the sum of the earlier tiles' sums (a few thousand words at most)
+    __shared__ uint32_t off_w[SCAN_THREADS / 32];
+    uint32_t part = 0;
+    for (uint32_t t = threadIdx.x; t < blockIdx.x; t += SCAN_THREADS) part += __ldg(bsum + t);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0) off_w[threadIdx.x >> 5] = part;
+    __syncthreads();
+    uint32_t off = 0;
+#pragma unroll
+    for (int w = 0; w < SCAN_THREADS / 32; w++) off += off_w[w];
     uint32_t total;
-    const uint32_t run = block_exclusive_scan(c4.x + c4.y + c4.z + c4.w, total) + bsum[blockIdx.x];
+    const uint32_t run = block_exclusive_scan(c4.x + c4.y + c4.z + c4.w, total) + off;
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) start[ncells] = off + total;
     const uint4 st4v = make_uint4(run, run + c4.x, run + c4.x + c4.y, run + c4.x + c4.y + c4.z);
     if (vec && base + 4 <= ncells) {
         *reinterpret_cast<uint4 *>(start + base) = st4v;
@@ -843,7 +840,6 @@ cudaError_t Launch<R>::scan(const DevBufs &b, uint32_t ncells, cudaStream_t st)
     const bool vec = ((reinterpret_cast<uintptr_t>(b.count) | reinterpret_cast<uintptr_t>(b.start) |
                        reinterpret_cast<uintptr_t>(b.cursor)) & 15u) == 0;
     k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, vec);
-    k_scan_top<<<1, SCAN_THREADS, 0, st>>>(b.bsum, nb, b.start, ncells);
     k_scan_apply<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, b.start, b.cursor, vec);
     return cudaGetLastError();
 }
