@@ -47,7 +47,7 @@ DIMS = (100, 100, 100)
 GRAVITY = (0.0, -9.81, 0.0)
 SEED = 1
 H32 = np.float32(0.0457)
-KERNELS_PER_STEP = 7  # scan reduce/top/apply, slot, rank+permute, density, forces
+KERNELS_PER_STEP = 6  # scan reduce and apply, slot, rank+permute, density, forces
 
 
 def workload_desc(form):
