@@ -75,6 +75,7 @@ struct sph_ctx {
     float trial_ms[3] = {0, 0, 0};
     cudaEvent_t on_ev[2] = {nullptr, nullptr};
     int graph_forces = -1;     // force variant captured in the graph
+    std::vector<unsigned char *> canaries;  // checked builds: the guard region after each array
 };
 
 namespace {
@@ -203,6 +204,15 @@ struct PoolItem {
     size_t bytes;
 };
 
+// Checked builds follow every array of the pool with a guard region of known bytes;
+// sph_debug_check reports any that changed (an out-of-bounds write that escaped the checks).
+#ifdef SPH_CHECKED
+constexpr size_t kCanaryBytes = 256;
+#else
+constexpr size_t kCanaryBytes = 0;
+#endif
+constexpr unsigned char kCanary = 0xA5;
+
 // The sub-arrays of a context's single device allocation (256-byte aligned); returns the
 // total size. Needs only the configuration (no CUDA call), so a create can be refused before
 // any device work and sph_memory_required can answer on the host.
@@ -240,7 +250,7 @@ size_t pool_layout(sph_ctx *c, std::vector<PoolItem> &items)
         {(void **) &b.inv, 4 * N},
     };
     size_t total = 0;
-    for (auto &it : items) total += (it.bytes + 255) & ~size_t(255);
+    for (auto &it : items) total += ((it.bytes + 255) & ~size_t(255)) + kCanaryBytes;
     return total;
 }
 
@@ -266,9 +276,15 @@ int allocate(sph_ctx *c)
                                           " bytes failed: " + cudaGetErrorString(e));
     }
     char *p = (char *) c->pool;
+    c->canaries.clear();
     for (auto &it : items) {
         *it.p = it.bytes ? (void *) p : nullptr;
         p += (it.bytes + 255) & ~size_t(255);
+        if (kCanaryBytes) {
+            c->canaries.push_back((unsigned char *) p);
+            CK(c, cudaMemsetAsync(p, kCanary, kCanaryBytes, c->stream));
+            p += kCanaryBytes;
+        }
     }
     CK(c, cudaMemsetAsync(b.count, 0, 4 * C, c->stream));
     CK(c, cudaMemsetAsync(b.aux, 0, r4 * N, c->stream));
@@ -634,6 +650,31 @@ int sph_batch_create(const sph_params *p, uint32_t n_scenes, const sph_scene_des
     } catch (...) {
         return fail(nullptr, SPH_ERR_NOMEM, "host exception in sph_batch_create");
     }
+}
+
+int sph_debug_check(sph_ctx *c, uint32_t *flags)
+{
+    if (!c || !flags) return c ? fail(c, SPH_ERR_ARG, "flags is NULL") : SPH_ERR_ARG;
+#ifndef SPH_CHECKED
+    return fail(c, SPH_ERR_UNSUPPORTED, "this library is built without checks (libsph_gb300_checked.so has them)");
+#else
+    CK(c, cudaSetDevice(c->device));
+    CK(c, cudaStreamSynchronize(c->stream));
+    *flags = 0;
+    CK(c, check_flags_kernels(flags));
+    CK(c, check_flags_mixed(flags));
+    CK(c, check_flags_handoff(flags));
+    std::vector<unsigned char> buf(kCanaryBytes);
+    for (unsigned char *g : c->canaries) {
+        CK(c, cudaMemcpy(buf.data(), g, kCanaryBytes, cudaMemcpyDeviceToHost));
+        for (unsigned char v : buf)
+            if (v != kCanary) {
+                *flags |= SPH_CHECK_CANARY;
+                break;
+            }
+    }
+    return SPH_OK;
+#endif
 }
 
 int sph_memory_required(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *scenes, uint64_t *bytes)

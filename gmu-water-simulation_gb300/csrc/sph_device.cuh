@@ -9,6 +9,37 @@
 
 namespace sph {
 
+// ---- checked builds (SPH_CHECKED): a failed index check sets a bit of this translation
+// unit's flag word and the access is skipped; sph_debug_check collects the words and verifies
+// the pool's canaries. Other builds compile the checks away.
+enum CheckBit : unsigned {
+    CHK_SORT = 1u,       // a counting-sort scatter target or cell range outside the particles
+    CHK_ROW = 2u,        // a neighbour row range outside the particles
+    CHK_NEIGHBOUR = 4u,  // a neighbour index from the masks outside its row
+    CHK_EGRESS = 8u,     // an id-ordered target outside the particles
+};
+#ifdef SPH_CHECKED
+static __device__ unsigned g_check_flags;
+__device__ __forceinline__ bool sph_check(bool ok, unsigned bit)
+{
+    if (!ok) atomicOr(&g_check_flags, bit);
+    return ok;
+}
+#define SPH_CHECK_ACCESSOR(name)                                                            \
+    cudaError_t name(uint32_t *out)                                                         \
+    {                                                                                       \
+        unsigned v = 0, z = 0;                                                              \
+        cudaError_t e = cudaMemcpyFromSymbol(&v, g_check_flags, sizeof v);                  \
+        if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_check_flags, &z, sizeof z);          \
+        *out |= v;                                                                          \
+        return e;                                                                           \
+    }
+#else
+__device__ __forceinline__ bool sph_check(bool, unsigned) { return true; }
+#define SPH_CHECK_ACCESSOR(name) \
+    cudaError_t name(uint32_t *) { return cudaSuccess; }
+#endif
+
 template <class R>
 struct alignas(4 * sizeof(R)) Vec4 {
     R x, y, z, w;

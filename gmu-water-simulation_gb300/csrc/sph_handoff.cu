@@ -108,6 +108,7 @@ __global__ void __launch_bounds__(256) k_id_index(const Vec4<R> *__restrict__ po
     if (i >= n) return;
     const uint32_t o = __ldg(scene_off + wbits(ldc4(pos + i).w)) + wbits(ldc4(vel + i).w);
     if (o < n) inv[o] = i;
+    else sph_check(false, CHK_EGRESS);
 }
 
 // 256 particles per block: the block's 3 x 256 floats of each array are assembled in shared
@@ -169,5 +170,7 @@ template cudaError_t launch_splat<float>(const DevBufs &, uint32_t, int, uint32_
                                          uint32_t, uint32_t, uint32_t *, float *, cudaStream_t);
 template cudaError_t launch_splat<double>(const DevBufs &, uint32_t, int, uint32_t, int, float, float, float, float,
                                           uint32_t, uint32_t, uint32_t *, float *, cudaStream_t);
+
+SPH_CHECK_ACCESSOR(check_flags_handoff)
 
 }  // namespace sph

@@ -170,6 +170,11 @@ cudaError_t launch_splat(const DevBufs &b, uint32_t n, int layout_sorted, uint32
                          float half_v, float scale_u, float scale_v, uint32_t width, uint32_t height,
                          uint32_t *count, float *depth, cudaStream_t st);
 
+// checked builds: OR each translation unit's device check flags into *out and clear them
+cudaError_t check_flags_kernels(uint32_t *out);
+cudaError_t check_flags_mixed(uint32_t *out);
+cudaError_t check_flags_handoff(uint32_t *out);
+
 // mixed-precision passes (sph_mixed.cu)
 cudaError_t mixed_permute(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, cudaStream_t st);
 cudaError_t mixed_density(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, cudaStream_t st);

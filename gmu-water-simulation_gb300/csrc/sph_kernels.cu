@@ -197,7 +197,8 @@ __global__ void __launch_bounds__(256) k_slot(const uint2 *__restrict__ cid_u, u
     uint32_t base = 0;
     if ((int) lane == leader) base = atomicAdd(cursor + cd.x, (uint32_t) __popc(peers));
     base = __shfl_sync(peers, base, leader);
-    tmp[base + (uint32_t) __popc(peers & ((1u << lane) - 1u))] = cd.y;
+    const uint32_t t = base + (uint32_t) __popc(peers & ((1u << lane) - 1u));
+    if (sph_check(t < n, CHK_SORT)) tmp[t] = cd.y;
 }
 
 template <class R>
@@ -212,9 +213,11 @@ __global__ void __launch_bounds__(256) k_rank_permute(const uint2 *__restrict__ 
     if (i >= n) return;
     const uint2 cd = cid_u[i];
     const uint32_t b = start[cd.x], e = start[cd.x + 1];
+    if (!sph_check(b <= e && e <= n, CHK_SORT)) return;
     uint32_t r = 0;
     for (uint32_t k = b; k < e; k++) r += tmp[k] < cd.y ? 1u : 0u;
     const uint32_t dst = b + r;
+    if (!sph_check(dst < e, CHK_SORT)) return;
     st4(pos_s + dst, ld4(pos_u + i));
     st4(vel_s + dst, ld4(vel_u + i));
 }
@@ -387,6 +390,7 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
             if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
             const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
             const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
             int w = 0;
             for (uint32_t cb = jb; cb < je; cb += 32, w++) {
                 // bit k of the chunk's word = candidate cb + k; bits enter at the top and
@@ -448,6 +452,7 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask(
             if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
             const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
             const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
             const uint32_t nw = (je - jb + 31) / 32;
             for (uint32_t w = 0; w < nw; w++) {
                 const uint32_t cb = jb + 32 * w;
@@ -464,7 +469,7 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask(
                 while (m) {
                     const uint32_t j = cb + (uint32_t) (__ffs(m) - 1);
                     m &= m - 1;
-                    if (j == i) continue;
+                    if (j == i || !sph_check(j < je, CHK_NEIGHBOUR)) continue;
                     if (REC) {
                         const Vec4<R> pj = ld4(frec + 2 * (size_t) j), vj = ld4(frec + 2 * (size_t) j + 1);
                         pair_terms<R>(pi, vi, qi, pj, vj, pj.w, vj.w, c, fpx, fpy, fpz, fvx, fvy, fvz);
@@ -512,6 +517,7 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask2(
             if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
             const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
             const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
             const uint32_t nw = (je - jb + 31) / 32;
             for (uint32_t w = 0; w < nw; w++) {
                 const uint32_t cb = jb + 32 * w;
@@ -532,6 +538,7 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask2(
                     const bool two = m != 0;
                     const uint32_t j1 = two ? cb + (uint32_t) (__ffs(m) - 1) : j0;
                     m &= m - 1;
+                    if (!sph_check(j0 < je && j1 < je, CHK_NEIGHBOUR)) continue;
                     Vec4<R> p0, v0, p1, v1;
                     R q0, inv0, q1, inv1;
                     if (REC) {
@@ -735,6 +742,7 @@ __global__ void __launch_bounds__(256) k_egress(const Vec4<R> *__restrict__ posL
     if (i < n_state) {
         const Vec4<R> pp = ldc4(posL + i), vv = ldc4(velL + i);
         const uint32_t o = __ldg(scene_off + wbits(pp.w)) + wbits(vv.w);
+        if (!sph_check(o < n_state, CHK_EGRESS)) return;
         xyz[3 * o] = pp.x; xyz[3 * o + 1] = pp.y; xyz[3 * o + 2] = pp.z;
         v[3 * o] = vv.x; v[3 * o + 1] = vv.y; v[3 * o + 2] = vv.z;
     }
@@ -984,5 +992,7 @@ cudaError_t launch_slot(const DevBufs &b, uint32_t n, cudaStream_t st)
 
 template struct Launch<float>;
 template struct Launch<double>;
+
+SPH_CHECK_ACCESSOR(check_flags_kernels)
 
 }  // namespace sph

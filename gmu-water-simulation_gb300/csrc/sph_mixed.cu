@@ -72,9 +72,11 @@ __global__ void __launch_bounds__(256) k_rank_permute_mixed(
     if (i >= n) return;
     const uint2 cd = cid_u[i];
     const uint32_t b = start[cd.x], e = start[cd.x + 1];
+    if (!sph_check(b <= e && e <= n, CHK_SORT)) return;
     uint32_t r = 0;
     for (uint32_t k = b; k < e; k++) r += tmp[k] < cd.y ? 1u : 0u;
     const uint32_t dst = b + r;
+    if (!sph_check(dst < e, CHK_SORT)) return;
     const Vec4<float> p = ld4(pos_u + i), lo = ld4(lo_u + i), v = ld4(vel_u + i);
     st4(pos_s + dst, p);
     st4(lo_s + dst, lo);
@@ -122,6 +124,7 @@ __global__ void __launch_bounds__(256) k_density_mixed(const Vec4<float> *__rest
             if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
             const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
             const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
             int w = 0;
             for (uint32_t cb = jb; cb < je; cb += 32, w++) {
                 // bit k of the chunk's word = candidate cb + k (bits enter at the top)
@@ -178,6 +181,7 @@ __global__ void __launch_bounds__(256, 4) k_forces_mixed(
             if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
             const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
             const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
             const uint32_t nw = (je - jb + 31) / 32;
             for (uint32_t w = 0; w < nw; w++) {
                 const uint32_t cb = jb + 32 * w;
@@ -195,7 +199,7 @@ __global__ void __launch_bounds__(256, 4) k_forces_mixed(
                 while (m) {
                     const uint32_t j = cb + (uint32_t) (__ffs(m) - 1);
                     m &= m - 1;
-                    if (j == i) continue;
+                    if (j == i || !sph_check(j < je, CHK_NEIGHBOUR)) continue;
                     float dx, dy_, dz_, vjx, vjy, vjz;
                     code_delta(gi, __ldg(gpos + j), dx, dy_, dz_);
                     unpack_half3(__ldg(gvel + j), vjx, vjy, vjz);
@@ -333,5 +337,7 @@ cudaError_t mixed_egress(const DevBufs &b, uint32_t n_state, uint32_t n_aux, uin
             b.st_vel, b.st_rho, b.st_p, b.st_acc);
     return cudaGetLastError();
 }
+
+SPH_CHECK_ACCESSOR(check_flags_mixed)
 
 }  // namespace sph

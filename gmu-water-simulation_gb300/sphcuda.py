@@ -17,7 +17,10 @@ import time
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "lib", "libsph_gb300.so")
+# SPH_LIBRARY selects another build of the library, e.g. lib/libsph_gb300_checked.so (bounds
+# checks and guarded allocations, reported by sph_debug_check)
+LIB_PATH = os.environ.get("SPH_LIBRARY") or os.path.join(HERE, "lib", "libsph_gb300.so")
+LIB_CHECKED_PATH = os.path.join(HERE, "lib", "libsph_gb300_checked.so")
 
 SPH_OK = 0
 SPH_ERR_ARG, SPH_ERR_CUDA, SPH_ERR_CAPACITY, SPH_ERR_STATE, SPH_ERR_NOMEM, SPH_ERR_UNSUPPORTED, SPH_ERR_DEVICE = (
@@ -27,7 +30,7 @@ SPH_FLAG_PROFILE, SPH_FLAG_RECORD_ACC, SPH_FLAG_ALL_PAIRS = 1, 2, 4
 
 # every symbol the header declares
 EXPORTS = (
-    "sph_params_default", "sph_create", "sph_batch_create", "sph_memory_required", "sph_destroy", "sph_last_error", "sph_device_name",
+    "sph_params_default", "sph_create", "sph_batch_create", "sph_memory_required", "sph_debug_check", "sph_destroy", "sph_last_error", "sph_device_name",
     "sph_stream", "sph_set_variant", "sph_get_variant", "sph_autotune", "sph_set_online_tuning", "sph_grid_build_noalloc",
     "sph_upload", "sph_append", "sph_emit_fountain", "sph_set_gravity", "sph_step", "sph_pass_grid", "sph_pass_density",
     "sph_pass_forces", "sph_pass_times", "sph_get_counts", "sph_num_scenes", "sph_num_particles",
@@ -84,6 +87,7 @@ def load(path=None):
                                    ctypes.POINTER(vp)]),
         "sph_memory_required": (i32, [ctypes.POINTER(sph_params), u32, ctypes.POINTER(sph_scene_desc),
                                       ctypes.POINTER(ctypes.c_uint64)]),
+        "sph_debug_check": (i32, [vp, up]),
         "sph_destroy": (None, [vp]),
         "sph_last_error": (ctypes.c_char_p, [vp]),
         "sph_device_name": (ctypes.c_char_p, [vp]),
@@ -335,6 +339,12 @@ class SphContext:
     def set_online_tuning(self, period):
         """Re-time the mask-driven force variants every `period` steps (0 = off)."""
         self._ck(load().sph_set_online_tuning(self.h, period))
+
+    def debug_check(self):
+        """Device check flags since the last call (checked library only; 0 = clean)."""
+        f = np.zeros(1, np.uint32)
+        self._ck(load().sph_debug_check(self.h, _p(f, ctypes.c_uint32)))
+        return int(f[0])
 
     def pass_times(self):
         ms = np.zeros(5, np.float64)

@@ -107,6 +107,20 @@ int sph_batch_create(const sph_params *p, uint32_t n_scenes, const sph_scene_des
  * exceeds the environment variable SPH_DEVICE_MEMORY_LIMIT (bytes; unset or 0 = no limit). */
 int sph_memory_required(const sph_params *params, uint32_t n_scenes, const sph_scene_desc *scenes, uint64_t *bytes);
 
+/* Checked builds (libsph_gb300_checked.so, compiled with SPH_CHECKED). Every counting-sort
+ * scatter target, neighbour row range, neighbour index from the masks and id-ordered target is
+ * bounds-checked on the device; a failed check skips the access and sets a flag. Every array
+ * of the context's pool is followed by a guard region of known bytes. This call waits for the
+ * context's work and returns the flags raised since the last call (clearing them), plus
+ * SPH_CHECK_CANARY if a guard region changed; 0 = clean. The other library returns
+ * SPH_ERR_UNSUPPORTED. */
+#define SPH_CHECK_SORT 1u
+#define SPH_CHECK_ROW 2u
+#define SPH_CHECK_NEIGHBOUR 4u
+#define SPH_CHECK_EGRESS 8u
+#define SPH_CHECK_CANARY 16u
+int sph_debug_check(sph_ctx *ctx, uint32_t *flags);
+
 void sph_destroy(sph_ctx *ctx);
 
 /* Last error message of ctx (or of the last failed create when ctx is NULL). */
