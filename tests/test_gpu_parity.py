@@ -484,6 +484,36 @@ def test_pinned_transfers_equal_staged_transfers(sphlib):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
 
 
+def test_fountain_emission_vs_oracle(sphlib, oracle_mod):
+    """Emitter steps against the oracle: after each device emission, one GPU step and one
+    oracle step from the same state, in the 1e-5 band. The jet is dense and fast, so whole
+    trajectories diverge chaotically within a few steps; each step is compared from the
+    common state instead. The first two steps also follow the oracle fed the host generator's
+    particles (the device emitter's bits) without resynchronising."""
+    box = (0.8, 0.8, 0.8)
+    args = dict(center=(0.0, -0.38, 0.0), radius=0.03, speed=1.5, sigma=0.05)
+    ctx = sphlib.SphContext(box, 4000, gravity=G981, flags=sphlib.SPH_FLAG_RECORD_ACC)
+    ctx.upload(np.zeros((0, 3), np.float32))
+    follow = oracle_mod.Oracle(box, oracle_mod.REF, threads=os.cpu_count(), gravity=G981)
+    for k in range(6):
+        ctx.emit_fountain(0, 21, k, 500, args["center"], args["radius"], args["speed"], args["sigma"])
+        before = ctx.download()
+        o = oracle_mod.Oracle(box, oracle_mod.REF, threads=os.cpu_count(), gravity=G981)
+        o.add(before["pos"], before["vel"])
+        o.step(1)
+        ctx.step(1)
+        got = ctx.download(acc=True)
+        assert_within(rel_errors({q: got[q] for q in ("rho", "p", "acc", "pos", "vel")}, o.state()),
+                      f"emission step {k}")
+        if k < 2:
+            xyz, vel = sphlib.fountain_emit(21, k, 500, **args)
+            follow.add(xyz, vel)
+            follow.step(1)
+            assert_within(rel_errors({q: got[q] for q in ("rho", "p", "acc", "pos", "vel")}, follow.state()),
+                          f"followed emission step {k}")
+    ctx.close()
+
+
 def test_device_emitter_equals_host_emitter(sphlib):
     """sph_emit_fountain generates on the device the same bits as the host generator, and a run
     fed by it equals a run fed by sph_append of the host-generated particles."""
@@ -684,6 +714,50 @@ def test_full_size_1m_properties(sphlib):
     np.testing.assert_allclose(s["rho_mean"], d["rho"].astype(np.float64).mean(), rtol=1e-9)
     ctx64.close()
     ctx.close()
+
+
+def test_full_size_16m_with_obstacles(sphlib):
+    """The largest configuration: 16,000,000 particles (400 x 200 x 200 lattice) in the
+    4 x 1 x 1 m box scaled x4.57, with 8 box obstacles. One plain FP32 step against an FP64
+    GPU step of the same state, compared on a 1M subsample (density 1e-5 relative,
+    acceleration 1e-5 of the subsample's largest), then conservation over 5 more steps."""
+    s_ = 4.57
+    box = (4 * s_, s_, s_)
+    pos = sphlib.dam_break_scene((400, 200, 200), box, seed=4)
+    rng = np.random.default_rng(48)
+    obs = []
+    for _ in range(8):
+        size = rng.uniform(0.05, 0.2, 3) * s_
+        cen = np.array([rng.uniform(0.05, 0.95) * box[0] / 2, rng.uniform(-0.5, 0.0) * box[1] / 2,
+                        rng.uniform(-0.9, 0.9) * box[2] / 2])
+        obs += list(cen - size / 2) + list(cen + size / 2)
+    obs = [np.array(obs, np.float32)]
+    n = pos.shape[0]
+    out = {}
+    for name, prec in (("f32", sphlib.SPH_PLAIN_F32), ("f64", sphlib.SPH_F64)):
+        ctx = sphlib.SphContext(box, n, precision=prec, gravity=G981, obstacles=obs,
+                                flags=sphlib.SPH_FLAG_RECORD_ACC)
+        ctx.upload(pos)
+        ctx.step(1)
+        if prec == sphlib.SPH_F64:
+            import ctypes
+            r = np.zeros(n); a = np.zeros((n, 3))
+            sphlib.load().sph_download_f64(ctx.h, None, None, ctypes.c_void_p(r.ctypes.data), None,
+                                           ctypes.c_void_p(a.ctypes.data))
+            out[name] = {"rho": r, "acc": a}
+        else:
+            d = ctx.download(acc=True)
+            out[name] = {"rho": d["rho"].astype(np.float64), "acc": d["acc"].astype(np.float64)}
+            ctx.step(5)
+            st = ctx.stats()
+            assert st["count"] == n and st["mass"] == float(np.float32(0.02)) * n
+            assert np.isfinite(st["kinetic"]) and np.isfinite(st["rho_max"])
+        ctx.close()
+    sub = np.random.default_rng(5).choice(n, 1_000_000, replace=False)
+    a, b = out["f32"], out["f64"]
+    assert np.max(np.abs(a["rho"][sub] - b["rho"][sub]) / b["rho"][sub]) < 1e-5
+    amax = np.max(np.linalg.norm(b["acc"][sub], axis=1))
+    assert np.max(np.linalg.norm(a["acc"][sub] - b["acc"][sub], axis=1)) / amax < 1e-5
 
 
 # ------------------------------------------------------------------------- launch variants
