@@ -187,18 +187,19 @@ int sph_pass_times(sph_ctx *ctx, double ms[5]);
  *            consecutive sorted particles per thread sharing one candidate scan
  *   forces:  0 = pair terms inside the candidate loop; 1, 2 = accepted neighbours compacted
  *            into a per-thread list of 32 / 64 entries in shared memory, pair terms after;
- *            3, 4 = the density pass records each particle's accepted neighbours as bit masks
- *            per row and the force pass visits only those (density_variant is then unused);
- *            4 trades registers for occupancy differently from 3; 5 and 6 load two accepted
- *            neighbours per iteration (with and without the register cap of 4); 7 is 6 reading each
- *            neighbour from one packed 32-byte force record written by the density pass; 8 and 9
- *            are 7 capped at 48 and 40 registers (5 and 6 blocks of 256 per SM) */
+ *            3..9 = the density pass records each particle's accepted neighbours as bit masks
+ *            per row and the force pass visits only those (density_variant is then unused):
+ *            3 and 4 one neighbour per iteration (4 capped at 64 registers); 5 and 6 two per
+ *            iteration (5 capped at 64); 7 is 6 reading each neighbour from one packed 32-byte
+ *            force record written by the density pass; 8 and 9 are 7 capped at 48 and 40
+ *            registers (5 and 6 blocks of 256 per SM). SPH_ERR_ARG for other numbers. */
 int sph_set_variant(sph_ctx *ctx, int32_t density_variant, int32_t forces_variant);
 int sph_get_variant(const sph_ctx *ctx, int32_t out[2]);
 
 /* Autotuner: one step in which every (density, forces) variant pair is timed on the current
- * state (both passes re-run from the same sorted inputs), the fastest pair is kept, and the choice is written to the cache file (SPH_TUNE_CACHE,
- * else $HOME/.cache/sph_gb300/tune.txt) under the device name, precision and particle-count
+ * state (both passes re-run from the same sorted inputs), the fastest pair is kept, and the
+ * choice is written to the cache file (SPH_TUNE_CACHE, else $HOME/.cache/sph_gb300/tune.txt)
+ * under the device name, precision and particle-count
  * bucket (floor(log2 n)). sph_upload applies a cached choice for its bucket. The simulation
  * advances by exactly one step; reps = timed repetitions per variant (>= 1). */
 int sph_autotune(sph_ctx *ctx, int32_t reps);
@@ -209,7 +210,7 @@ int sph_autotune(sph_ctx *ctx, int32_t reps);
  * calls), one real step runs with each of the record-reading force variants 7, 8 and 9, timed
  * with events on the context's stream (one host synchronisation per trial step), and the
  * fastest is kept until the next trial. All of them compute the same bits, so the results do
- * not depend on the choice. Applies while the current force variant is mask-driven (3..7).
+ * not depend on the choice. Applies while the current force variant is mask-driven (3..9).
  * period 0 turns it off (the default); otherwise period >= 3. Not for mixed or all-pairs
  * contexts (SPH_ERR_STATE). */
 int sph_set_online_tuning(sph_ctx *ctx, int32_t period);
