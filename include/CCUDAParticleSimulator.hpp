@@ -211,6 +211,16 @@ public:
     double updateCollisions() { return 0.0; }  // fused into updateForces
     double integrate() { return 0.0; }         // fused into updateForces
 
+    // Front-end handoff without a synchronising readback: queue the id-ordered positions into
+    // xyz (pinned host memory for an asynchronous copy; 3 floats per particle) and carry on
+    // stepping; handoffWait() returns once they have landed.
+    void handoffPositions(float *xyz) { check(sph_handoff_async(m_ctx, xyz, nullptr)); }
+    void handoffWait() { check(sph_handoff_wait(m_ctx)); }
+
+    // Re-time the force variants every `period` steps on real steps (0 = off); every variant
+    // gives the same bits, so only the speed changes.
+    void setOnlineTuning(int period) { check(sph_set_online_tuning(m_ctx, period)); }
+
 private:
     static std::string num(double v)
     {

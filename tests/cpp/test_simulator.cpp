@@ -57,6 +57,18 @@ int main(int argc, char **argv)
             CHECK(std::string(line).rfind("GPU CUDA;", 0) == 0 && semis == 4);
             std::fclose(f);
         }
+        // the handoff delivers the state of the moment it was queued while stepping goes on
+        {
+            std::vector<float> now_xyz, v0, r0;
+            sim.readState(now_xyz, v0, r0);
+            std::vector<float> handed(now_xyz.size(), -1.0f);
+            sim.handoffPositions(handed.data());
+            sim.step();
+            sim.handoffWait();
+            CHECK(handed == now_xyz);
+        }
+        sim.setOnlineTuning(3);
+        for (int k = 0; k < 4; k++) sim.step();
         // an out-of-order pass makes the next step fail: the simulator stops and signals
         std::string msg;
         sim.errorOccured = [&](const char *m) { msg = m; };
