@@ -183,12 +183,17 @@ void *pinned_view(const void *p)
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+// The scene-offset table on the device, copied only when the scene counts changed since the
+// last copy (uploads and downloads of an unchanged batch skip the small pageable copy).
 int upload_scene_off(sph_ctx *c)
 {
-    c->scene_off_host.assign(c->sc.size() + 1, 0);
-    for (size_t s = 0; s < c->sc.size(); s++) c->scene_off_host[s + 1] = c->scene_off_host[s] + c->sc[s].count;
-    CK(c, cudaMemcpyAsync(c->b.scene_off, c->scene_off_host.data(), c->scene_off_host.size() * sizeof(uint32_t),
-                          cudaMemcpyHostToDevice, c->stream));
+    std::vector<uint32_t> off(c->sc.size() + 1, 0);
+    for (size_t s = 0; s < c->sc.size(); s++) off[s + 1] = off[s] + c->sc[s].count;
+    if (off == c->scene_off_host) return SPH_OK;
+    // pageable source: staged before the call returns, so the local array may go
+    CK(c, cudaMemcpyAsync(c->b.scene_off, off.data(), off.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                          c->stream));
+    c->scene_off_host = off;  // only once the copy is queued
     return SPH_OK;
 }
 
