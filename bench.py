@@ -30,6 +30,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -119,17 +120,17 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device=0):
+    def __init__(self, device=0, path=None):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else "/tmp/sph_bench_clocks.csv"
+        # the raw samples: a caller-chosen file (--clocks-log), else a temporary one
+        self.path = path or os.path.join(tempfile.gettempdir(), f"sph_bench_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -397,6 +398,8 @@ def main():
     ap.add_argument("--threads", type=int, default=0, help="host threads of the reference arm (0 = all)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", default=None, help="pin launch variants 'density,forces' instead of autotuning")
+    ap.add_argument("--clocks-log", default=None,
+                    help="file for the raw nvidia-smi clock samples of the timed region (default: a temporary file)")
     ap.add_argument("--save-state", default=None,
                     help="write the final positions and velocities of the timed run (npz)")
     ap.add_argument("--init-state", default=None,
@@ -471,7 +474,7 @@ def main():
     torch.cuda.synchronize()
 
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
-    clocks = ClockSampler(0)
+    clocks = ClockSampler(0, args.clocks_log)
     clocks.start()
     time.sleep(0.3)
     torch.cuda.synchronize()
