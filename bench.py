@@ -17,6 +17,8 @@ value : particle-steps/s with the state resident in HBM; L2 is flushed (a 512 Mi
         library's own stream.
 e2e   : the same metric through the public C ABI with pinned host buffers: every step
         uploads positions and velocities, steps once, and downloads them.
+mixed : the mixed-precision form on the same workload and steps, timed the same way, with
+        mixed / plain and its own one-step error against FP64 (--no-mixed skips it).
 roofline: algorithmic bytes of the dominant kernel / its event-timed duration, against
         the measured HBM copy bandwidth.
 cpu_baseline: the oracle (restatement of the reference's serial CPU step) on 1 host core
@@ -216,6 +218,40 @@ def fp64_error(sphcuda, ctx, form, N):
             "pos_max_abs_m": float(np.max(np.abs(np.asarray(a["pos"], np.float64) - b["pos"])))}
 
 
+def mixed_leg(sphcuda, torch, pos, vel0, steps, warmup, flush, dev):
+    """The mixed-precision form on the same workload and the same number of steps, timed as the
+    plain run (per step: L2 flush, then the three passes between CUDA events on the library's
+    stream), with its own one-step FP64 check from its final state."""
+    N = pos.shape[0]
+    ctx = sphcuda.SphContext(BOX, N, precision=sphcuda.SPH_MIXED, gravity=GRAVITY)
+    ctx.upload(pos, vel0)
+    ctx.step(1)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
+
+    def one(ev=None):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        if ev is not None:
+            ev[0].record(ext)
+        ctx.pass_grid()
+        ctx.pass_density()
+        ctx.pass_forces()
+        if ev is not None:
+            ev[1].record(ext)
+
+    for _ in range(warmup):
+        one()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(steps)]
+    torch.cuda.synchronize()
+    for k in range(steps):
+        one(evs[k])
+    torch.cuda.synchronize()
+    total_ms = sum(e[0].elapsed_time(e[1]) for e in evs)
+    check = fp64_error(sphcuda, ctx, sphcuda.SPH_MIXED, N)
+    ctx.close()
+    return N * steps / (total_ms / 1000.0), total_ms / steps, check
+
+
 def run_reference(args):
     """--impl reference: the oracle restatement of the reference's CPU step on all cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -398,6 +434,8 @@ def main():
     ap.add_argument("--threads", type=int, default=0, help="host threads of the reference arm (0 = all)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", default=None, help="pin launch variants 'density,forces' instead of autotuning")
+    ap.add_argument("--no-mixed", action="store_true",
+                    help="skip the mixed-precision leg of the plain run (mixed over plain on the same steps)")
     ap.add_argument("--clocks-log", default=None,
                     help="file for the raw nvidia-smi clock samples of the timed region (default: a temporary file)")
     ap.add_argument("--save-state", default=None,
@@ -539,6 +577,14 @@ def main():
            "same_final_state_as_resident_run": same}
     ctx.close()
 
+    mixed = None
+    if args.form == "plain" and not args.no_mixed:
+        mv, mms, mcheck = mixed_leg(sphcuda, torch, pos, vel0, args.steps, args.warmup, flush, dev)
+        mixed = {"value": mv, "unit": UNIT, "ms_per_step": mms, "mixed_over_plain": mv / value,
+                 "steps": args.steps, "fp64_check": mcheck,
+                 "form": "16-bit cell-relative neighbour positions, FP16 neighbour velocities, compensated "
+                         "density sums, hi/lo positions"}
+
     cpu = None
     if not args.no_cpu_baseline:
         try:
@@ -563,6 +609,7 @@ def main():
                           "frac": step_bytes / (total_ms / args.steps / 1000) / 1e9 / peak},
         "passes_ms": {"grid": mean(grid_ms), "density": mean(dens_ms), "forces": mean(forc_ms)},
         "e2e": e2e,
+        "mixed": mixed,
         "cpu_baseline": cpu,
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "launch_variant": {"density": variant[0], "forces": main_v,
