@@ -488,8 +488,8 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask(
 // loaded before either's terms are added, so two gathers are in flight at once and the loop
 // overhead is paid once per pair. The terms are still added one neighbour at a time in
 // candidate order (the sums are the same bits as the other forms).
-template <class R, int MINB, bool REC>
-__global__ void __launch_bounds__(256, MINB) k_forces_mask2(
+template <class R, int MINB, bool REC, int BLOCK = 256>
+__global__ void __launch_bounds__(BLOCK, MINB) k_forces_mask2(
     const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
     const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
     uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ frec,
@@ -934,6 +934,11 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
         k_forces_mask2<R, 6, true><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
                                                                  b.masks, (const Vec4<R> *) b.frec, po, vo, ao,
                                                                  b.cid_u, b.count);
+        break;
+    case 10:
+        k_forces_mask2<R, 12, true, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles,
+                                                                       n, c, b.masks, (const Vec4<R> *) b.frec, po, vo,
+                                                                       ao, b.cid_u, b.count);
         break;
     case 1:
         k_forces_list<R, 32, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
