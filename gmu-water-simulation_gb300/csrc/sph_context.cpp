@@ -511,17 +511,17 @@ float elapsed(cudaEvent_t a, cudaEvent_t b)
 }
 
 // ---- online tuning: the mask-driven force variants compute the same bits, so real steps can
-// try each in turn. The candidates are three record-reading variants (8, 9: the same kernel at
-// 48 and 40 registers; 10: 9 in blocks of 128 threads), whose order depends on how
-// latency-bound the pass is. Every online_period steps, one step runs with each candidate,
+// try each in turn. The candidates are three record-reading variants (9: the kernel at 40
+// registers in blocks of 256 threads; 10 and 11: at 40 and 48 registers in blocks of 128),
+// whose order depends on how latency-bound the pass is. Every online_period steps, one step runs with each candidate,
 // timed from the start of its grid pass to the end of its force pass; the fastest is kept
 // until the next trial. A trial step waits for its own end (one host synchronisation per
 // candidate).
-constexpr int kOnlineCand[3] = {8, 9, 10};
+constexpr int kOnlineCand[3] = {9, 10, 11};
 
 bool online_active(const sph_ctx *c)
 {
-    return c->online_period > 0 && !is_mixed(c) && c->tune.forces_mode >= 3 && c->tune.forces_mode <= 10;
+    return c->online_period > 0 && !is_mixed(c) && c->tune.forces_mode >= 3 && c->tune.forces_mode <= 11;
 }
 
 // before a step: start a due trial and set this step's candidate
@@ -553,7 +553,7 @@ int online_end_step(sph_ctx *c)
 }
 
 bool valid_density(int v) { return v == 0 || v == 1 || v == 2 || v == 4; }
-bool valid_forces(int v) { return v >= 0 && v <= 10; }
+bool valid_forces(int v) { return v >= 0 && v <= 11; }
 
 int bucket_of(uint64_t n)
 {
@@ -1024,6 +1024,7 @@ int sph_autotune(sph_ctx *c, int32_t reps)
     cfgs.push_back({0, 8});
     cfgs.push_back({0, 9});
     cfgs.push_back({0, 10});
+    cfgs.push_back({0, 11});
     float best = 1e30f;
     int bd = c->tune.density_p, bf = c->tune.forces_mode;
     for (const Cfg &g : cfgs) {

@@ -112,12 +112,12 @@ struct MixConsts {
 //   density_p : 0 = one particle per thread, first form; 1/2/4 = blocked branchless form
 //               with that many consecutive particles per thread
 //   forces_mode: 0 = pair terms inside the candidate loop; 1/2 = compacted neighbour list
-//               of 32/64 entries per thread in shared memory; 3..10 = driven by the neighbour
+//               of 32/64 entries per thread in shared memory; 3..11 = driven by the neighbour
 //               masks that the density pass then writes (density_p is ignored): 3/4 one
 //               neighbour per iteration without/with a 64-register cap, 5/6 two per
 //               iteration with/without it, 7 as 6 with each neighbour's terms read from one
 //               packed force record (two 16-byte loads from one 32-byte record), 8 and 9 as
-//               7 at 48 and 40 registers, 10 as 9 in blocks of 128 threads
+//               7 at 48 and 40 registers, 10 and 11 as 9 and 8 in blocks of 128 threads
 struct Tune {
     static constexpr int ALL_PAIRS = 16;  // both passes over every particle of the scene
     int density_p = 2;

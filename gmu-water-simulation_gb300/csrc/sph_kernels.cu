@@ -940,6 +940,11 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
                                                                        n, c, b.masks, (const Vec4<R> *) b.frec, po, vo,
                                                                        ao, b.cid_u, b.count);
         break;
+    case 11:
+        k_forces_mask2<R, 10, true, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles,
+                                                                       n, c, b.masks, (const Vec4<R> *) b.frec, po, vo,
+                                                                       ao, b.cid_u, b.count);
+        break;
     case 1:
         k_forces_list<R, 32, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
                                                                   po, vo, ao, b.cid_u, b.count);

@@ -187,13 +187,13 @@ int sph_pass_times(sph_ctx *ctx, double ms[5]);
  *            consecutive sorted particles per thread sharing one candidate scan
  *   forces:  0 = pair terms inside the candidate loop; 1, 2 = accepted neighbours compacted
  *            into a per-thread list of 32 / 64 entries in shared memory, pair terms after;
- *            3..10 = the density pass records each particle's accepted neighbours as bit masks
+ *            3..11 = the density pass records each particle's accepted neighbours as bit masks
  *            per row and the force pass visits only those (density_variant is then unused):
  *            3 and 4 one neighbour per iteration (4 capped at 64 registers); 5 and 6 two per
  *            iteration (5 capped at 64); 7 is 6 reading each neighbour from one packed 32-byte
  *            force record written by the density pass; 8 and 9 are 7 capped at 48 and 40
- *            registers (5 and 6 blocks of 256 per SM); 10 is 9 launched in blocks of 128
- *            threads (12 per SM). SPH_ERR_ARG for other numbers. */
+ *            registers (5 and 6 blocks of 256 per SM); 10 and 11 are 9 and 8 launched in
+ *            blocks of 128 threads (12 and 10 per SM). SPH_ERR_ARG for other numbers. */
 int sph_set_variant(sph_ctx *ctx, int32_t density_variant, int32_t forces_variant);
 int sph_get_variant(const sph_ctx *ctx, int32_t out[2]);
 
@@ -208,10 +208,10 @@ int sph_autotune(sph_ctx *ctx, int32_t reps);
 /* Online tuning of the force variant for a state that changes over a run (a collapsing dam
  * break packs ~4x more neighbours per particle after a few hundred steps than at the start,
  * and the fastest variant changes with it). Every `period` steps (sph_step or the pass
- * calls), one real step runs with each of the record-reading force variants 8, 9 and 10,
+ * calls), one real step runs with each of the record-reading force variants 9, 10 and 11,
  * timed with events on the context's stream (one host synchronisation per trial step), and the
  * fastest is kept until the next trial. All of them compute the same bits, so the results do
- * not depend on the choice. Applies while the current force variant is mask-driven (3..10).
+ * not depend on the choice. Applies while the current force variant is mask-driven (3..11).
  * period 0 turns it off (the default); otherwise period >= 3. Not for mixed or all-pairs
  * contexts (SPH_ERR_STATE). */
 int sph_set_online_tuning(sph_ctx *ctx, int32_t period);
