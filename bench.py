@@ -98,12 +98,13 @@ MASK_BYTES = 36  # 9 rows x one 32-bit mask word per particle (rest density)
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernels
 # per force variant, from one ncu capture of an early step of this workload (L2 flushed before
 # each replay); profiles/step_kernels_dam_break_1m.md (variant 4) and
-# profiles/k_density_mask_k_forces_mask2_records_dam_break_1m.md (variants 7, 8, 9, 10)
+# profiles/k_density_mask_k_forces_mask2_records_dam_break_1m.md (variants 7 to 11)
 TRAFFIC = {("k_forces", 4): 102.44e6, ("k_density", 4): 21.43e6,
            ("k_forces", 7): 133.90e6, ("k_density", 7): 58.08e6,
            ("k_forces", 8): 133.22e6, ("k_density", 8): 58.17e6,
            ("k_forces", 9): 135.43e6, ("k_density", 9): 58.08e6,
-           ("k_forces", 10): 135.40e6, ("k_density", 10): 58.26e6}
+           ("k_forces", 10): 135.40e6, ("k_density", 10): 58.26e6,
+           ("k_forces", 11): 133.28e6, ("k_density", 11): 57.91e6}
 
 
 def load_peak():
