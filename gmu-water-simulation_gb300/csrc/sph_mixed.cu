@@ -5,8 +5,10 @@
 //    of 16): code = (c mod 8) << 13 | q, where c = floor((p + box/2) / h) is the particle's
 //    unclamped cell along that axis and q its offset inside that cell in units of h / 8192.
 //    The 16-bit two's-complement difference of two codes is the displacement in those units,
-//    exactly, whenever the particles are less than 7 h apart along the axis (every neighbour
-//    candidate is, unless a particle has been pushed more than ~5 h outside the box);
+//    exactly, when the particles are less than 4 h apart along the axis; from 4 h to 7 h apart
+//    it wraps to a magnitude above h, so the neighbour test still rejects the pair (every
+//    neighbour candidate is within 7 h unless a particle has been pushed more than ~5 h
+//    outside the box);
 //  - neighbour velocities are gathered in FP16 (8 bytes instead of 16);
 //  - density sums are compensated FP32 sums: each 32-candidate chunk is summed, and the chunk
 //    sums are added with Kahan compensation;
