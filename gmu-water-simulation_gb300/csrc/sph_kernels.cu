@@ -519,11 +519,15 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_forces_mask2(
             const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
             if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
             const uint32_t nw = (je - jb + 31) / 32;
+            // the row's recorded words loaded together at the start of the row
+            const uint32_t *mr = masks + (size_t) (r * MASK_WORDS) * n + i;
+            const uint32_t w0 = nw > 0 ? __ldg(mr) : 0u, w1 = nw > 1 ? __ldg(mr + n) : 0u;
+            const uint32_t w2 = nw > 2 ? __ldg(mr + 2 * (size_t) n) : 0u, w3 = nw > 3 ? __ldg(mr + 3 * (size_t) n) : 0u;
             for (uint32_t w = 0; w < nw; w++) {
                 const uint32_t cb = jb + 32 * w;
                 uint32_t m = 0;
                 if (w < (uint32_t) MASK_WORDS) {
-                    m = __ldg(masks + (size_t) (r * MASK_WORDS + w) * n + i);
+                    m = w == 0 ? w0 : w == 1 ? w1 : w == 2 ? w2 : w3;
                 } else {  // beyond the recorded chunks: test the candidates here
                     const uint32_t ce = min(je, cb + 32u);
                     for (uint32_t j = ce; j-- > cb;) {
