@@ -36,6 +36,8 @@ struct SceneHost {
 
 enum State { EMPTY = 0, HASHED = 1, SORTED = 2, DENSE = 3 };
 
+constexpr int kOnlineN = 3;  // force variants tried by online tuning (one trial step each)
+
 thread_local std::string g_create_error;
 
 }  // namespace
@@ -72,7 +74,7 @@ struct sph_ctx {
     int online_period = 0;     // steps between trials; 0 = off
     uint64_t steps_run = 0;    // whole steps run by this context
     int trial = -1;            // candidate being timed in this step, -1 = none
-    float trial_ms[3] = {0, 0, 0};
+    float trial_ms[kOnlineN] = {};  // one per online candidate
     cudaEvent_t on_ev[2] = {nullptr, nullptr};
     int graph_forces = -1;     // force variant captured in the graph
     std::vector<unsigned char *> canaries;  // checked builds: the guard region after each array
@@ -517,7 +519,7 @@ float elapsed(cudaEvent_t a, cudaEvent_t b)
 // timed from the start of its grid pass to the end of its force pass; the fastest is kept
 // until the next trial. A trial step waits for its own end (one host synchronisation per
 // candidate).
-constexpr int kOnlineCand[3] = {9, 10, 11};
+constexpr int kOnlineCand[kOnlineN] = {9, 10, 11};
 
 bool online_active(const sph_ctx *c)
 {
@@ -543,9 +545,9 @@ int online_end_step(sph_ctx *c)
     CK(c, cudaEventRecord(c->on_ev[1], c->stream));
     CK(c, cudaEventSynchronize(c->on_ev[1]));
     c->trial_ms[c->trial] = elapsed(c->on_ev[0], c->on_ev[1]);
-    if (++c->trial < 3) return SPH_OK;
+    if (++c->trial < kOnlineN) return SPH_OK;
     int best = 0;
-    for (int k = 1; k < 3; k++)
+    for (int k = 1; k < kOnlineN; k++)
         if (c->trial_ms[k] < c->trial_ms[best]) best = k;
     c->tune.forces_mode = kOnlineCand[best];
     c->trial = -1;
@@ -966,7 +968,7 @@ int sph_step(sph_ctx *c, int32_t nsteps)
 int sph_set_online_tuning(sph_ctx *c, int32_t period)
 {
     if (!c) return SPH_ERR_ARG;
-    if (period != 0 && period < 3) return fail(c, SPH_ERR_ARG, "period must be 0 (off) or at least 3 steps");
+    if (period != 0 && period < kOnlineN) return fail(c, SPH_ERR_ARG, "period must be 0 (off) or at least 3 steps");
     if (period && (is_mixed(c) || (c->prm.flags & SPH_FLAG_ALL_PAIRS)))
         return fail(c, SPH_ERR_STATE, "this context has no force variants to tune");
     if (c->trial >= 0) return fail(c, SPH_ERR_STATE, "a tuning trial is in progress");
