@@ -210,6 +210,10 @@ class Oracle:
             ob = np.ascontiguousarray(obstacles, np.float32).reshape(-1, 6)
             L.orc_set_obstacles(self.h, ob.shape[0], _f(ob))
 
+    def set_gravity(self, g):
+        """setGravityVector (src/CBaseParticleSimulator.cpp:111-114): used from the next step."""
+        lib().orc_set_gravity(self.h, *[ctypes.c_float(v) for v in g])
+
     def close(self):
         if self.h:
             lib().orc_destroy(self.h)

@@ -213,6 +213,50 @@ def test_batch_equals_single_scenes(sphlib):
     batch.close()
 
 
+def test_gravity_change_between_steps(sphlib, oracle_mod):
+    """setGravityVector between steps (src/CBaseParticleSimulator.cpp:111-114; the G key,
+    :154-179), for one scene of a batch or for all of them, takes effect at the next step. The
+    batch with its gravity changed mid-run equals each scene run alone with the same changes,
+    bit for bit, and the step after the last change matches the oracle under the new gravity."""
+    O = oracle_mod
+    boxes = [(0.4, 0.4, 0.4), (0.5, 0.3, 0.4)]
+    parts = [O.reference_dam_break(0.4), sphlib.dam_break_scene((8, 6, 8), boxes[1], seed=3)]
+    counts = [p.shape[0] for p in parts]
+    off = np.concatenate([[0], np.cumsum(counts)])
+    g1, g2 = (2.0, -5.0, 1.0), (0.0, -3.0, -2.0)
+    batch = sphlib.SphContext(boxes, counts, gravity=G981, flags=sphlib.SPH_FLAG_RECORD_ACC)
+    batch.upload(np.concatenate(parts), None, counts)
+    batch.step(3)
+    batch.set_gravity(g1, scene=1)
+    batch.step(2)
+    batch.set_gravity(g2)
+    mid = batch.download()
+    batch.step(1)
+    got = batch.download(acc=True)
+    batch.close()
+    for s, p in enumerate(parts):
+        one = sphlib.SphContext(boxes[s], p.shape[0], gravity=G981, flags=sphlib.SPH_FLAG_RECORD_ACC)
+        one.upload(p)
+        one.step(3)
+        if s == 1:
+            one.set_gravity(g1)
+        one.step(2)
+        one.set_gravity(g2)
+        one.step(1)
+        alone = one.download(acc=True)
+        one.close()
+        for k in ("pos", "vel", "rho", "p", "acc"):
+            assert np.array_equal(got[k][off[s]:off[s + 1]], alone[k]), (s, k)
+        o = O.Oracle(boxes[s], O.REF, threads=1, gravity=G981)
+        o.add(mid["pos"][off[s]:off[s + 1]], mid["vel"][off[s]:off[s + 1]])
+        o.set_gravity(g2)
+        o.step(1)
+        ref = o.state()
+        o.close()
+        assert_within(rel_errors({k: got[k][off[s]:off[s + 1]] for k in ("pos", "vel", "rho", "p", "acc")}, ref),
+                      f"scene {s} after the gravity change")
+
+
 def test_determinism(sphlib):
     pos = c0_scene(sphlib)
     a = gpu_run(sphlib, C0_BOX, pos, steps=25, gravity=G981)

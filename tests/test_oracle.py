@@ -275,3 +275,25 @@ def test_oracle_brute_matches_reference_brute_kernels(oracle_mod, case):
                             "ascale": A[inside]}))
     assert_within(errs, case["name"])
     assert max(errs.values()) < 0.1, errs
+
+
+def test_oracle_gravity_change(oracle_mod):
+    """Oracle.set_gravity (setGravityVector, src/CBaseParticleSimulator.cpp:111-114) applies from
+    the next step: changing it on a running simulation equals building one with that gravity
+    from the same state."""
+    O = oracle_mod
+    pos = O.reference_dam_break(0.4)
+    a = O.Oracle(0.4, O.REF, threads=1)
+    a.add(pos)
+    a.step(2)
+    mid = a.state()
+    a.set_gravity((1.0, -4.0, 0.5))
+    a.step(1)
+    b = O.Oracle(0.4, O.REF, threads=1, gravity=(1.0, -4.0, 0.5))
+    b.add(mid["pos"], mid["vel"])
+    b.step(1)
+    sa, sb = a.state(), b.state()
+    assert not np.array_equal(sa["pos"], mid["pos"])
+    # the same method from the same state; only the within-cell order can differ (REF lists)
+    assert np.max(np.abs(sa["pos"] - sb["pos"])) < 1e-6
+    assert np.max(np.abs(sa["acc"] - sb["acc"]) / (sb["ascale"][:, None])) < 1e-5
