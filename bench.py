@@ -405,9 +405,13 @@ def run_config(args):
             steps_done[0] += 1
         return work
 
-    variant = ctx.autotune(reps=2) if ctx.n else (0, 3)
-    if args.form != "mixed":
-        ctx.set_online_tuning(50)
+    if args.variant:
+        ctx.set_variant(*[int(v) for v in args.variant.split(",")])
+        variant = ctx.variant()
+    else:
+        variant = ctx.autotune(reps=2) if ctx.n else (0, 3)
+        if args.form != "mixed":
+            ctx.set_online_tuning(50)
     warm = []
     advance(max(args.warmup, 3), warm)
     ms = []

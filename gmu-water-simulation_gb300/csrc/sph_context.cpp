@@ -36,7 +36,7 @@ struct SceneHost {
 
 enum State { EMPTY = 0, HASHED = 1, SORTED = 2, DENSE = 3 };
 
-constexpr int kOnlineN = 3;  // force variants tried by online tuning (one trial step each)
+constexpr int kOnlineN = 4;  // force variants tried by online tuning (one trial step each)
 
 thread_local std::string g_create_error;
 
@@ -513,13 +513,14 @@ float elapsed(cudaEvent_t a, cudaEvent_t b)
 }
 
 // ---- online tuning: the mask-driven force variants compute the same bits, so real steps can
-// try each in turn. The candidates are three record-reading variants (9: the kernel at 40
-// registers in blocks of 256 threads; 10 and 11: at 40 and 48 registers in blocks of 128),
-// whose order depends on how latency-bound the pass is. Every online_period steps, one step runs with each candidate,
+// try each in turn. The candidates are four record-reading variants of one kernel (7: no
+// register cap, blocks of 256 threads; 9: 40 registers, blocks of 256; 10 and 11: 40 and 48
+// registers, blocks of 128), whose order depends on how latency-bound the pass is: the
+// collapsing dam break settles on 9 or 10, the dense fountain on 7. Every online_period steps, one step runs with each candidate,
 // timed from the start of its grid pass to the end of its force pass; the fastest is kept
 // until the next trial. A trial step waits for its own end (one host synchronisation per
 // candidate).
-constexpr int kOnlineCand[kOnlineN] = {9, 10, 11};
+constexpr int kOnlineCand[kOnlineN] = {7, 9, 10, 11};
 
 bool online_active(const sph_ctx *c)
 {
@@ -968,7 +969,7 @@ int sph_step(sph_ctx *c, int32_t nsteps)
 int sph_set_online_tuning(sph_ctx *c, int32_t period)
 {
     if (!c) return SPH_ERR_ARG;
-    if (period != 0 && period < kOnlineN) return fail(c, SPH_ERR_ARG, "period must be 0 (off) or at least 3 steps");
+    if (period != 0 && period < kOnlineN) return fail(c, SPH_ERR_ARG, "period must be 0 (off) or at least 4 steps");
     if (period && (is_mixed(c) || (c->prm.flags & SPH_FLAG_ALL_PAIRS)))
         return fail(c, SPH_ERR_STATE, "this context has no force variants to tune");
     if (c->trial >= 0) return fail(c, SPH_ERR_STATE, "a tuning trial is in progress");

@@ -208,11 +208,11 @@ int sph_autotune(sph_ctx *ctx, int32_t reps);
 /* Online tuning of the force variant for a state that changes over a run (a collapsing dam
  * break packs ~4x more neighbours per particle after a few hundred steps than at the start,
  * and the fastest variant changes with it). Every `period` steps (sph_step or the pass
- * calls), one real step runs with each of the record-reading force variants 9, 10 and 11,
+ * calls), one real step runs with each of the record-reading force variants 7, 9, 10 and 11,
  * timed with events on the context's stream (one host synchronisation per trial step), and the
  * fastest is kept until the next trial. All of them compute the same bits, so the results do
  * not depend on the choice. Applies while the current force variant is mask-driven (3..11).
- * period 0 turns it off (the default); otherwise period >= 3. Not for mixed or all-pairs
+ * period 0 turns it off (the default); otherwise period >= 4. Not for mixed or all-pairs
  * contexts (SPH_ERR_STATE). */
 int sph_set_online_tuning(sph_ctx *ctx, int32_t period);
 

@@ -67,7 +67,7 @@ int main(int argc, char **argv)
             sim.handoffWait();
             CHECK(handed == now_xyz);
         }
-        sim.setOnlineTuning(3);
+        sim.setOnlineTuning(4);
         for (int k = 0; k < 4; k++) sim.step();
         // an out-of-order pass makes the next step fail: the simulator stops and signals
         std::string msg;
