@@ -22,3 +22,19 @@ def test_reference_arm_line():
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
     assert "workload" in line["config"]
+
+
+def test_byte_model_matches_the_documented_totals():
+    """bench.py's algorithmic bytes per step: 360 N + 48 C with the force records (variants 7 and
+    up), the density pass 116 N + 4 C and the force pass 156 N + 12 C; the 1M dam break's cell
+    count is 110 x 110 x 55."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    N, C = 1_000_000, bench.grid_cells(bench.BOX)
+    assert C == 110 * 110 * 55
+    for v in (7, 9, 10, 11):
+        ab = bench.alg_bytes(N, C, 4, v)
+        assert ab["density"] == 116 * N + 4 * C and ab["forces"] == 156 * N + 12 * C
+        assert sum(ab.values()) == 360 * N + 48 * C
+        assert ("k_forces", v) in bench.TRAFFIC and ("k_density", v) in bench.TRAFFIC
