@@ -434,7 +434,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="plain", choices=["plain", "f64", "mixed"])
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=10,
+                    help="accepted and ignored: the end-to-end leg always runs the timed run's own steps, "
+                         "so that its final state can be compared with the resident run's")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-budget", type=float, default=90.0)
     ap.add_argument("--threads", type=int, default=0, help="host threads of the reference arm (0 = all)")
