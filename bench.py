@@ -5,12 +5,12 @@
 
 Workload: the 1,000,000-particle dam break (100^3 lattice at 0.5 h spacing, +-1% seeded
 jitter, anchored at the min corner of a 5 x 5 x 2.5 m box -- the 20^3 / 1 x 1 x 0.5 m
-scene scaled x5 to keep its fill), gravity -9.81, the reference's constants. A step is
-one pass of the whole step (grid build, density, forces + walls + integration) over all
-particles, launched through the C ABI. By default the timed region is the configuration's
-whole 500-step run after the warm-up steps: the column collapses under gravity and
-densities (and neighbour counts) rise during the run, so a shorter --steps measures only
-its early part.
+scene scaled x5 to keep its fill), gravity -9.81, the reference's constants, 500 steps. A
+step is one pass of the whole step (grid build, density, forces + walls + integration) over
+all particles, launched through the C ABI. The column collapses under gravity and densities
+(and neighbour counts) rise during the run, so the K timed steps are spread evenly over the
+configuration's whole 500-step run (every 500/K-th step; all of them for K >= 500); the steps
+between them run untimed.
 
 value : particle-steps/s with the state resident in HBM; L2 is flushed (a 512 MiB write)
         before every timed step, and the step is timed with CUDA events on the
@@ -19,12 +19,18 @@ e2e   : the same metric through the public C ABI with pinned host buffers: every
         uploads positions and velocities, steps once, and downloads them.
 mixed : the mixed-precision form on the same workload and steps, timed the same way, with
         mixed / plain and its own one-step error against FP64 (--no-mixed skips it).
-roofline: algorithmic bytes of the dominant kernel / its event-timed duration, against
-        the measured HBM copy bandwidth.
+batch : the 256-scene batch (particle counts log-uniform in [2000, 64000]), plain and mixed,
+        K timed steps spread over its 1,000-step run, with mixed / plain and the error of
+        one step against FP64 (--no-batch skips it).
+roofline: compulsory bytes of the dominant kernel (each array it must touch read or written
+        once) / its event-timed duration, against the measured HBM copy bandwidth; beside it
+        the same with the implementation's own bytes (masks, force records) and an issue
+        roofline from the kernel's measured instruction count.
 cpu_baseline: the oracle (restatement of the reference's serial CPU step) on 1 host core
         for a bounded sample of the same workload.
 --impl reference: the same restatement on all host cores (OpenMP over particles, the
-        grid re-binning serial as in the reference), the same workload and metric.
+        grid re-binning serial as in the reference), the same workload and metric; its
+        inputs come from the oracle's own scene restatement, not from the product library.
 """
 import argparse
 import json
@@ -50,31 +56,58 @@ DIMS = (100, 100, 100)
 GRAVITY = (0.0, -9.81, 0.0)
 SEED = 1
 H32 = np.float32(0.0457)
-KERNELS_PER_STEP = 6  # scan reduce and apply, slot, rank+permute, density, forces
+KERNELS_PER_STEP = 7  # scan reduce and apply, slot, crowded-cell sort, rank+permute, density, forces
+RUN_STEPS = 500        # the configuration's run
+BATCH_RUN_STEPS = 1000  # the 256-scene batch's run
+SM_COUNT = 152
+ISSUE_PER_SM_CLK = 4   # warp instructions issued per SM and clock (four schedulers)
 
 
-def workload_desc(form):
+def workload_desc(form, steps=None):
+    k = steps or RUN_STEPS
+    run = max(k, RUN_STEPS)
     return {
         "workload": "dam break, 1,000,000 particles (100^3 lattice, 0.5h spacing, +-1% jitter), "
-                    "box 5 x 5 x 2.5 m, 110 x 110 x 55 cells",
+                    "box 5 x 5 x 2.5 m, 110 x 110 x 55 cells, 500-step run",
         "form": form,
         "particles": 1_000_000,
         "cells": 665_500,
-        "steps_from": "initial lattice, after one autotune step and the warm-up steps",
+        "steps_from": f"{k} timed steps spread evenly over a {run}-step run (every {run / k:g}-th step) that "
+                      "starts from the initial lattice after one autotune step and the warm-up steps",
         "l2": "flushed before every timed step (512 MiB write)",
         "parallelism": "single GPU",
     }
+
+
+def timed_steps(k, run):
+    """Indices of the k timed steps, spread evenly over a run of `run` steps (run >= k)."""
+    return sorted({(i * run) // k for i in range(k)})
 
 
 def grid_cells(box):
     return int(np.prod([int(np.ceil(np.float32(b) / H32)) for b in box]))
 
 
+def compulsory_bytes(N, C, form="plain"):
+    """Algorithmic (compulsory) DRAM bytes of the step's passes: the state each pass must read
+    and write once, nothing of the implementation's own intermediates. Plain FP32 per particle:
+    density reads the position (16) and writes rho, p (8): 24; forces + walls + integration read
+    position, velocity (16 each) and rho, p (8) and write position and velocity (16 each): 72;
+    the whole step 196 B per particle plus 12 B per cell for the scan. The mixed form gathers
+    8-byte codes and FP16 velocities: density 8 + 8 = 16, forces 32 read + 32 written = 64, the
+    step about 115 B per particle. FP64 doubles the plain figures."""
+    if form == "mixed":
+        return {"density": 16 * N, "forces": 64 * N, "step": 115 * N + 12 * C}
+    k = 2 if form == "f64" else 1
+    return {"density": 24 * k * N, "forces": 72 * k * N, "step": 196 * k * N + 12 * C}
+
+
 def alg_bytes(N, C, rs=4, forces_variant=4):
-    """Compulsory DRAM bytes of each kernel of one step: every array it must touch,
-    read or written once (neighbour re-reads are cache hits). rs = bytes per real.
-    Force variants 7 and up also have the density pass read velocities and write the packed force
-    records, which the force pass then reads."""
+    """The implementation's own DRAM bytes of each kernel of one step: every array it touches,
+    read or written once (neighbour re-reads are cache hits), including its intermediates (the
+    neighbour masks, the packed force records). rs = bytes per real. Force variants 7 and up
+    also have the density pass read velocities and write the packed force records, which the
+    force pass then reads."""
     r4 = 4 * rs
     rec = 3 * r4 * N if forces_variant >= 7 else 0  # velocity read + 2 x r4 record written
     return {
@@ -95,16 +128,15 @@ def alg_bytes(N, C, rs=4, forces_variant=4):
 
 MASK_BYTES = 36  # 9 rows x one 32-bit mask word per particle (rest density)
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernels
-# per force variant, from one ncu capture of an early step of this workload (L2 flushed before
-# each replay); profiles/step_kernels_dam_break_1m.md (variant 4) and
-# profiles/k_density_mask_k_forces_mask2_records_dam_break_1m.md (variants 7 to 11)
-TRAFFIC = {("k_forces", 4): 102.44e6, ("k_density", 4): 21.43e6,
-           ("k_forces", 7): 133.90e6, ("k_density", 7): 58.08e6,
-           ("k_forces", 8): 133.22e6, ("k_density", 8): 58.17e6,
-           ("k_forces", 9): 135.43e6, ("k_density", 9): 58.08e6,
-           ("k_forces", 10): 135.40e6, ("k_density", 10): 58.26e6,
-           ("k_forces", 11): 133.28e6, ("k_density", 11): 57.91e6}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) and warp instructions
+# (smsp__inst_executed.sum) per launch of the dominant kernels in the compressed column (step ~254
+# of this workload, where most of the run is spent), one ncu capture of each kernel alone with
+# force variant 10: profiles/k_forces_mask2_variant10_k_density_mask_step254_dam_break_1m.md
+TRAFFIC = {"k_forces": 194.83e6, "k_density": 102.56e6}
+ISSUE = {"k_forces": 388.12e6, "k_density": 312.25e6}
+TRAFFIC_SOURCE = ("ncu, one launch at step ~254 (the compressed column), force variant 10: "
+                  "profiles/k_forces_mask2_variant10_k_density_mask_step254_dam_break_1m.md")
+ISSUE_SOURCE = TRAFFIC_SOURCE
 
 
 def load_peak():
@@ -204,6 +236,8 @@ def fp64_error(sphcuda, ctx, form, N):
     out = {}
     for name, prec in (("form", form), ("f64", sphcuda.SPH_F64)):
         c = sphcuda.SphContext(BOX, N, precision=prec, gravity=GRAVITY, flags=sphcuda.SPH_FLAG_RECORD_ACC)
+        if prec != sphcuda.SPH_F64:  # the measured run's grid
+            c.set_cell_multiple(ctx.cell_multiple())
         c.upload(x32, v32)
         c.step(1)
         out[name] = c.download(acc=True)
@@ -220,38 +254,121 @@ def fp64_error(sphcuda, ctx, form, N):
             "pos_max_abs_m": float(np.max(np.abs(np.asarray(a["pos"], np.float64) - b["pos"])))}
 
 
-def mixed_leg(sphcuda, torch, pos, vel0, steps, warmup, flush, dev):
-    """The mixed-precision form on the same workload and the same number of steps, timed as the
-    plain run (per step: L2 flush, then the three passes between CUDA events on the library's
-    stream), with its own one-step FP64 check from its final state."""
+def timed_run(ctx, torch, ext, flush, warmup, k, run, on_step=None):
+    """Steps a context through `warmup` untimed steps and then a `run`-step run of which the k
+    steps of timed_steps(k, run) are timed: per timed step, L2 flushed, then the three passes
+    between CUDA events on the library's stream. Returns the per-step event times
+    [(grid, density, forces), ...] and the force variant of each timed step."""
+    def passes(evs=None):
+        if evs is not None:
+            evs[0].record(ext)
+        ctx.pass_grid()
+        if evs is not None:
+            evs[1].record(ext)
+        ctx.pass_density()
+        if evs is not None:
+            evs[2].record(ext)
+        ctx.pass_forces()
+        if evs is not None:
+            evs[3].record(ext)
+
+    for _ in range(warmup):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        passes()
+    torch.cuda.synchronize()
+    want = set(timed_steps(k, run))
+    evs, used = [], []
+    if on_step:
+        on_step("start")
+    for q in range(run):
+        if q in want:
+            with torch.cuda.stream(ext):
+                flush.zero_()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            passes(e)
+            evs.append(e)
+            used.append(ctx.variant()[1])
+        else:
+            passes()
+    torch.cuda.synchronize()
+    if on_step:
+        on_step("stop")
+    times = [(e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), e[2].elapsed_time(e[3])) for e in evs]
+    return times, used
+
+
+def mixed_leg(sphcuda, torch, pos, vel0, steps, warmup, flush, dev, run=RUN_STEPS):
+    """The mixed-precision form on the same workload, the same warm-up and the same timed steps
+    of the same run, timed as the plain run, with its own one-step FP64 check from its final
+    state."""
     N = pos.shape[0]
     ctx = sphcuda.SphContext(BOX, N, precision=sphcuda.SPH_MIXED, gravity=GRAVITY)
     ctx.upload(pos, vel0)
-    ctx.step(1)
+    # one autotune step (the plain run's first step), then online tuning of the mixed form's
+    # force launch forms, as the plain run does with its own
+    ctx.autotune(reps=3)
+    ctx.set_online_tuning(50)
     ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
-
-    def one(ev=None):
-        with torch.cuda.stream(ext):
-            flush.zero_()
-        if ev is not None:
-            ev[0].record(ext)
-        ctx.pass_grid()
-        ctx.pass_density()
-        ctx.pass_forces()
-        if ev is not None:
-            ev[1].record(ext)
-
-    for _ in range(warmup):
-        one()
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(steps)]
-    torch.cuda.synchronize()
-    for k in range(steps):
-        one(evs[k])
-    torch.cuda.synchronize()
-    total_ms = sum(e[0].elapsed_time(e[1]) for e in evs)
+    times, _ = timed_run(ctx, torch, ext, flush, warmup, steps, max(steps, run))
+    total_ms = sum(sum(t) for t in times)
     check = fp64_error(sphcuda, ctx, sphcuda.SPH_MIXED, N)
+    check["cell_multiple"] = ctx.cell_multiple()
+    check["passes_ms"] = {k: sum(t[q] for t in times) / len(times) for q, k in enumerate(("grid", "density", "forces"))}
     ctx.close()
-    return N * steps / (total_ms / 1000.0), total_ms / steps, check
+    return N * len(times) / (total_ms / 1000.0), total_ms / len(times), check
+
+
+def batch_scenes(sphcuda, seed=3):
+    """The 256 dam-break scenes of the batch configuration: (boxes, positions, counts)."""
+    dims, boxes = sphcuda.batch_plan(256, seed=seed)
+    parts = [sphcuda.dam_break_scene(tuple(int(x) for x in d), tuple(float(x) for x in b), s)
+             for s, (d, b) in enumerate(zip(dims, boxes))]
+    return [tuple(float(x) for x in b) for b in boxes], np.concatenate(parts), [p.shape[0] for p in parts]
+
+
+def batch_fp64_error(sphcuda, ctx, form, boxes, counts):
+    """Max relative density error over all particles of all scenes, one step from the batch's
+    final state, against an FP64 context of the same scenes."""
+    st = ctx.download()
+    out = {}
+    for name, prec in (("form", form), ("f64", sphcuda.SPH_F64)):
+        c = sphcuda.SphContext(boxes, counts, precision=prec, gravity=GRAVITY)
+        if prec != sphcuda.SPH_F64:  # the measured run's grid
+            c.set_cell_multiple(ctx.cell_multiple())
+        c.upload(st["pos"], st["vel"], counts)
+        c.step(1)
+        out[name] = c.download()["rho"].astype(np.float64)
+        c.close()
+    return float(np.max(np.abs(out["form"] - out["f64"]) / np.abs(out["f64"])))
+
+
+def batch_leg(sphcuda, torch, steps, warmup, flush, dev):
+    """The 256-scene batch, plain FP32 and mixed: one launch per pass over all scenes, the same
+    per-step timing as the headline (L2 flushed before every timed step), k timed steps spread
+    over the 1,000-step run, launch variants picked by sph_autotune (and online tuning where the
+    form has force variants)."""
+    boxes, pos, counts = batch_scenes(sphcuda)
+    N = int(sum(counts))
+    res = {"workload": f"256 dam-break scenes, {N:,} particles, counts log-uniform in [2000, 64000], aspect "
+                       "per axis uniform in [0.5, 2] (seed 3), 1,000-step run",
+           "particles": N, "steps": steps, "run": max(steps, BATCH_RUN_STEPS)}
+    for name, prec in (("plain", sphcuda.SPH_PLAIN_F32), ("mixed", sphcuda.SPH_MIXED)):
+        ctx = sphcuda.SphContext(boxes, counts, precision=prec, gravity=GRAVITY)
+        ctx.upload(pos, None, counts)
+        ctx.autotune(reps=2)
+        ctx.set_online_tuning(50)
+        ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
+        times, used = timed_run(ctx, torch, ext, flush, warmup, steps, max(steps, BATCH_RUN_STEPS))
+        total_ms = sum(sum(t) for t in times)
+        res[name] = {"value": N * len(times) / (total_ms / 1000.0), "ms_per_step": total_ms / len(times),
+                     "cell_multiple": ctx.cell_multiple(), "forces_variants": sorted(set(used)),
+                     "passes_ms": {k: sum(t[q] for t in times) / len(times)
+                                   for q, k in enumerate(("grid", "density", "forces"))},
+                     "rho_max_rel_vs_fp64": batch_fp64_error(sphcuda, ctx, prec, boxes, counts)}
+        ctx.close()
+    res["mixed_over_plain"] = res["mixed"]["value"] / res["plain"]["value"]
+    return res
 
 
 def run_reference(args):
@@ -259,14 +376,21 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    import sphcuda
     from oracle import oracle as O
+    from oracle import scenes as OS
 
     O.build()
     threads = args.threads or os.cpu_count() or 1
     if args.config == "dam1m":
-        box, pos, obstacles, desc, emit = BOX, sphcuda.dam_break_scene(DIMS, BOX, SEED), None, None, None
+        # the scene from the oracle's own restatement of the lattice: this arm loads no product code
+        box, pos, obstacles, desc, emit = BOX, OS.dam_break(DIMS, BOX, SEED), None, None, None
+    elif args.config == "dam8k":
+        box, obstacles, emit = (1.0, 1.0, 0.5), None, None
+        pos = OS.dam_break((20, 20, 20), box, 0)
+        desc = "dam break, 8,000 particles (20^3 lattice), box 1 x 1 x 0.5 m"
     else:
+        import sphcuda  # the other configurations' generators (batch plan, emitter, obstacles)
+
         boxes, pos, counts, caps, obs, emit, desc = build_config(sphcuda, args.config)
         if len(boxes) != 1:
             print(json.dumps({"impl": "reference", "unavailable": f"config {args.config}: the oracle runs one "
@@ -282,6 +406,8 @@ def run_reference(args):
         # the emitter (host generator, the same particles as the device emitter) is the
         # step's first phase, as generateParticles is in the reference
         if emit is not None and o.n + emit["per_step"] <= emit["cap"]:
+            import sphcuda
+
             xyz, vel = sphcuda.fountain_emit(7, emitted[0], emit["per_step"], emit["center"], emit["radius"],
                                              emit["speed"], emit["sigma"])
             o.add(xyz, vel)
@@ -289,7 +415,7 @@ def run_reference(args):
         o.step(1)
         return o.n
 
-    warm = min(args.warmup, 3)
+    warm = args.warmup
     for _ in range(warm):
         one_step()
     # each timed step is one full step of the scene; stop at K steps or the time budget
@@ -311,13 +437,15 @@ def run_reference(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": done,
         "warmup": warm, "ms_per_step": 1000 * el / done, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_desc("reference CPU step (oracle restatement), float/double as the reference"),
+        "config": dict(workload_desc("reference CPU step (oracle restatement), float/double as the reference"),
+                       steps_from=f"the first {done} steps after {warm} warm-up steps from the initial lattice "
+                                  "(a bounded sample of the run)"),
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{done} of {args.steps} requested steps (time budget {args.ref_budget:.0f} s) of "
                                    f"the 1,000,000-particle dam break after {warm} warm-up steps; density/force "
                                    f"passes on {threads} threads (bit-identical to 1 thread), grid re-binning "
-                                   "serial"},
+                                   "serial; scene from the oracle's lattice restatement"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -376,6 +504,8 @@ def run_config(args):
     form = {"plain": sphcuda.SPH_PLAIN_F32, "f64": sphcuda.SPH_F64, "mixed": sphcuda.SPH_MIXED}[args.form]
     boxes, pos, counts, caps, obstacles, emit, desc = build_config(sphcuda, args.config)
     ctx = sphcuda.SphContext(boxes, caps, precision=form, gravity=GRAVITY, obstacles=obstacles)
+    if args.cell_multiple or args.variant:  # pinned choices (else the autotuner's)
+        ctx.set_cell_multiple(args.cell_multiple or 1)
     ctx.upload(pos, None, counts)
     ext = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda:0"))
     steps_done = [0]
@@ -410,8 +540,7 @@ def run_config(args):
         variant = ctx.variant()
     else:
         variant = ctx.autotune(reps=2) if ctx.n else (0, 3)
-        if args.form != "mixed":
-            ctx.set_online_tuning(50)
+        ctx.set_online_tuning(50)
     warm = []
     advance(max(args.warmup, 3), warm)
     ms = []
@@ -420,7 +549,8 @@ def run_config(args):
     finite = bool(np.isfinite(st["rho_mean"]))
     line = {"metric": METRIC, "value": work / (sum(ms) / 1000.0), "unit": UNIT, "config": {"workload": desc,
             "form": args.form, "particles_final": ctx.n, "scenes": len(boxes)}, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": sum(ms) / args.steps, "launch_variant": list(variant),
+            "warmup": max(args.warmup, 3), "ms_per_step": sum(ms) / args.steps,
+            "launch_variant": list(ctx.variant()), "cell_multiple": ctx.cell_multiple(),
             "finite": finite, "rho_mean_scene0": st["rho_mean"], "l2": "not flushed (replayed steps)"}
     ctx.close()
     print(json.dumps(line), flush=True)
@@ -453,6 +583,12 @@ def main():
                          "run) instead of the initial lattice, e.g. to profile the compressed column")
     ap.add_argument("--config", default="dam1m", choices=["dam1m", "dam8k", "batch256", "fountain", "dam16m"],
                     help="dam1m is the benchmark line; the others are measured separately")
+    ap.add_argument("--run", type=int, default=RUN_STEPS,
+                    help="steps of the run over which the timed steps are spread (default: the configuration's "
+                         "500; e.g. a few steps to profile a state given by --init-state)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 256-scene batch leg")
+    ap.add_argument("--cell-multiple", type=int, default=0,
+                    help="pin the step grid's cell multiple (1: cells of h, 2: cells of h/2) instead of autotuning it")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -484,60 +620,42 @@ def main():
     ctx = sphcuda.SphContext(BOX, N, precision=form, gravity=GRAVITY)
     ctx.upload(pos, vel0)
     # one untimed step picks the launch variants (all variants compute the same bits)
+    if args.cell_multiple or args.variant:  # pinned choices (else the autotuner's)
+        ctx.set_cell_multiple(args.cell_multiple or 1)
     if args.variant:
         ctx.set_variant(*[int(v) for v in args.variant.split(",")])
         ctx.step(1)
         variant = ctx.variant()
     else:
         variant = ctx.autotune(reps=3)
-        # the state changes over the run (the column compresses): re-time the mask-driven force
-        # variants every 50 steps on real steps (all give the same bits)
-        if args.form != "mixed":
-            ctx.set_online_tuning(50)
+        # the state changes over the run (the column compresses): re-time the force variants
+        # every 50 steps on real steps (all give the same bits)
+        ctx.set_online_tuning(50)
+    cell_mult = ctx.cell_multiple()
     ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    used = []  # force variant of each timed step (online tuning may change it)
-
-    def one_step(evs=None):
-        if evs is not None:
-            evs[0].record(ext)
-        ctx.pass_grid()
-        if evs is not None:
-            used.append(ctx.variant()[1])
-            evs[1].record(ext)
-        ctx.pass_density()
-        if evs is not None:
-            evs[2].record(ext)
-        ctx.pass_forces()
-        if evs is not None:
-            evs[3].record(ext)
-
-    for _ in range(args.warmup):
-        with torch.cuda.stream(ext):
-            flush.zero_()
-        one_step()
-    torch.cuda.synchronize()
-
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    run = max(args.steps, args.run)
     clocks = ClockSampler(0, args.clocks_log)
-    clocks.start()
-    time.sleep(0.3)
-    torch.cuda.synchronize()
-    t_wall0 = time.perf_counter()
-    for k in range(args.steps):
-        with torch.cuda.stream(ext):
-            flush.zero_()
-        one_step(evs[k])
-    torch.cuda.synchronize()
-    t_wall = time.perf_counter() - t_wall0
+    t_wall = [0.0]
+
+    def on_step(what):
+        if what == "start":
+            clocks.start()
+            time.sleep(0.3)
+            torch.cuda.synchronize()
+            t_wall[0] = time.perf_counter()
+        else:
+            t_wall[0] = time.perf_counter() - t_wall[0]
+
+    times, used = timed_run(ctx, torch, ext, flush, args.warmup, args.steps, run, on_step)
     clk = clocks.stop()
-    grid_ms = [e[0].elapsed_time(e[1]) for e in evs]
-    dens_ms = [e[1].elapsed_time(e[2]) for e in evs]
-    forc_ms = [e[2].elapsed_time(e[3]) for e in evs]
-    step_ms = [e[0].elapsed_time(e[3]) for e in evs]
-    total_ms = sum(step_ms)
-    value = N * args.steps / (total_ms / 1000.0)
+    K = len(times)
+    grid_ms = [t[0] for t in times]
+    dens_ms = [t[1] for t in times]
+    forc_ms = [t[2] for t in times]
+    total_ms = sum(sum(t) for t in times)
+    value = N * K / (total_ms / 1000.0)
     stats = ctx.stats()
     assert stats["count"] == N and np.isfinite(stats["rho_mean"])
     resident_final = ctx.download()
@@ -545,21 +663,33 @@ def main():
         np.savez(args.save_state, pos=resident_final["pos"], vel=resident_final["vel"])
     fp64_check = fp64_error(sphcuda, ctx, form, N)
 
-    # bytes of each timed step by the variant it ran, against the summed event times
-    ab_steps = [alg_bytes(N, C, rs, v) for v in used]
-    ab = {k: sum(a[k] for a in ab_steps) / len(ab_steps) for k in ab_steps[0]}
-    main_v = max(set(used), key=used.count)
     peak, peak_src = load_peak()
     mean = lambda xs: sum(xs) / len(xs)
     dom = "forces" if mean(forc_ms) >= mean(dens_ms) else "density"
     dom_ms = mean(forc_ms) if dom == "forces" else mean(dens_ms)
-    achieved = ab[dom] / (dom_ms / 1000.0) / 1e9
-    traffic = TRAFFIC.get((f"k_{dom}", main_v)) if args.form == "plain" else None
-    step_bytes = sum(ab.values())
+    main_v = max(set(used), key=used.count)
+    # compulsory bytes (the roofline) and the implementation's own bytes, by the variant each
+    # timed step ran
+    comp = compulsory_bytes(N, C, args.form)
+    ab_steps = [alg_bytes(N, C, rs, v) for v in used]
+    ab = {k: sum(a[k] for a in ab_steps) / len(ab_steps) for k in ab_steps[0]}
+    achieved = comp[dom] / (dom_ms / 1000.0) / 1e9
+    impl_achieved = ab[dom] / (dom_ms / 1000.0) / 1e9
+    traffic = TRAFFIC.get(f"k_{dom}") if args.form == "plain" else None
+    inst = ISSUE.get(f"k_{dom}") if args.form == "plain" else None
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    issue = None
+    if inst:
+        issue_peak = SM_COUNT * ISSUE_PER_SM_CLK * sm_mhz * 1e6
+        issue = {"warp_inst_per_launch": inst, "achieved": inst / (dom_ms / 1000.0), "peak": issue_peak,
+                 "unit": "warp instructions/s", "frac": inst / (dom_ms / 1000.0) / issue_peak,
+                 "source": ISSUE_SOURCE}
+    step_ms = total_ms / K
 
     # ---- end to end through the C ABI with pinned host buffers, the same state sequence:
-    # from the initial upload, one untimed step, W warm-up steps, then K timed steps, each
-    # uploading positions and velocities, stepping once and downloading them
+    # from the initial upload, one untimed step, W warm-up steps, then the run, every step
+    # uploading positions and velocities, stepping once and downloading them; the run's sampled
+    # steps are timed on the host
     bufs = [(torch.from_numpy(pos.copy()).pin_memory(), torch.from_numpy(vel0.copy()).pin_memory()),
             (torch.empty((N, 3), dtype=torch.float32).pin_memory(),
              torch.empty((N, 3), dtype=torch.float32).pin_memory())]
@@ -573,25 +703,36 @@ def main():
 
     for k in range(1 + args.warmup):
         e2e_step(k)
-    t0 = time.perf_counter()
-    for k in range(1 + args.warmup, 1 + args.warmup + args.steps):
-        e2e_step(k)
-    e2e_s = time.perf_counter() - t0
-    last = bufs[(1 + args.warmup + args.steps) % 2]
+    want = set(timed_steps(args.steps, run))
+    e2e_s = 0.0
+    for q in range(run):
+        k = 1 + args.warmup + q
+        if q in want:
+            t0 = time.perf_counter()
+            e2e_step(k)
+            e2e_s += time.perf_counter() - t0
+        else:
+            e2e_step(k)
+    last = bufs[(1 + args.warmup + run) % 2]
     same = bool(np.array_equal(last[0].numpy(), resident_final["pos"]))
-    e2e = {"value": N * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 24 * N,
+    e2e = {"value": N * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 24 * N,
            "d2h_bytes_per_step": 24 * N,
-           "path": "sph_upload (pinned xyz+vel) -> sph_step(1) -> sph_download (pinned xyz+vel), host timer",
+           "path": "sph_upload (pinned xyz+vel) -> sph_step(1) -> sph_download (pinned xyz+vel), host timer, "
+                   "the same sampled steps of the same run",
            "same_final_state_as_resident_run": same}
     ctx.close()
 
     mixed = None
     if args.form == "plain" and not args.no_mixed:
-        mv, mms, mcheck = mixed_leg(sphcuda, torch, pos, vel0, args.steps, args.warmup, flush, dev)
+        mv, mms, mcheck = mixed_leg(sphcuda, torch, pos, vel0, args.steps, args.warmup, flush, dev, run)
         mixed = {"value": mv, "unit": UNIT, "ms_per_step": mms, "mixed_over_plain": mv / value,
-                 "steps": args.steps, "fp64_check": mcheck,
+                 "steps": K, "fp64_check": mcheck,
                  "form": "16-bit cell-relative neighbour positions, FP16 neighbour velocities, compensated "
                          "density sums, hi/lo positions"}
+
+    batch = None
+    if args.form == "plain" and not args.no_batch and not args.init_state:
+        batch = batch_leg(sphcuda, torch, args.steps, args.warmup, flush, dev)
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -604,28 +745,36 @@ def main():
             cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "error": repr(exc)}
 
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": args.warmup,
+        "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.form == "f64" else "f32", "data": "synthetic (seeded lattice, no dataset)",
-        "config": dict(workload_desc({"plain": "plain FP32", "f64": "FP64", "mixed": "mixed precision"}[args.form]),
-                       **({"initial_state": args.init_state} if args.init_state else {})),
+        "config": dict(workload_desc({"plain": "plain FP32", "f64": "FP64", "mixed": "mixed precision"}[args.form],
+                                     K),
+                       **({"initial_state": args.init_state, "run": run} if args.init_state else {})),
         "fp64_check": fp64_check,
         "roofline": {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
-                     "alg_bytes_per_launch": ab[dom], "launch_ms": dom_ms},
-        "step_roofline": {"alg_bytes_per_step": step_bytes, "achieved_gbs": step_bytes / (total_ms / args.steps / 1000) / 1e9,
-                          "frac": step_bytes / (total_ms / args.steps / 1000) / 1e9 / peak},
+                     "frac": achieved / peak, "peak_source": peak_src,
+                     "bytes": "compulsory: each array the pass must touch read or written once",
+                     "alg_bytes_per_launch": comp[dom], "launch_ms": dom_ms,
+                     "traffic": traffic, "traffic_source": TRAFFIC_SOURCE if traffic else None,
+                     "impl_bytes_per_launch": ab[dom], "frac_impl_bytes": impl_achieved / peak,
+                     "issue": issue},
+        "step_roofline": {"alg_bytes_per_step": comp["step"], "achieved_gbs": comp["step"] / (step_ms / 1000) / 1e9,
+                          "frac": comp["step"] / (step_ms / 1000) / 1e9 / peak,
+                          "impl_bytes_per_step": sum(ab.values()),
+                          "frac_impl_bytes": sum(ab.values()) / (step_ms / 1000) / 1e9 / peak},
         "passes_ms": {"grid": mean(grid_ms), "density": mean(dens_ms), "forces": mean(forc_ms)},
         "e2e": e2e,
         "mixed": mixed,
+        "batch": batch,
         "cpu_baseline": cpu,
-        "gpu_launches": KERNELS_PER_STEP * args.steps,
-        "launch_variant": {"density": variant[0], "forces": main_v,
+        "gpu_launches": KERNELS_PER_STEP * K,
+        "launch_variant": {"density": variant[0], "forces": main_v, "cell_multiple": cell_mult,
                            "forces_steps": {str(v): used.count(v) for v in sorted(set(used))},
                            "picked_by": "--variant" if args.variant else
-                           "sph_autotune, then online tuning every 50 steps"},
+                           "sph_autotune (cell multiple and variants), then online tuning every 50 steps"},
         "clocks": clk,
-        "wall_s_timed_region": t_wall,
+        "wall_s_timed_region": t_wall[0],
     }
     print(json.dumps(line), flush=True)
     return 0

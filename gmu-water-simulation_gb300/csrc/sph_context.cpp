@@ -47,7 +47,9 @@ struct sph_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::vector<SceneHost> sc;
-    uint64_t ctot = 0, ncap = 0;
+    uint64_t ctot = 0, ncap = 0;  // cells of the step grid (all scenes), particle capacity
+    uint64_t ctot_ref = 0;        // cells of the reference grid (cells of size h)
+    uint64_t ctot_cap = 0;        // cells the grid arrays hold: the finest grid this context may use
     uint32_t n = 0;         // particles held (including appended ones)
     uint32_t n_sorted = 0;  // particles covered by the last grid pass
     uint32_t n_forced = 0;  // particles covered by the last force pass (recorded accelerations)
@@ -117,7 +119,7 @@ MixConsts make_mix(const sph_params &p)
 size_t r4_bytes(const sph_ctx *c) { return is_f64(c) ? 32 : 16; }
 
 template <class R>
-Consts<R> make_consts(const sph_params &p)
+Consts<R> make_consts(const sph_params &p, int cell_mult = 1)
 {
     Consts<R> c{};
     const double h = (double) p.h;
@@ -138,28 +140,38 @@ Consts<R> make_consts(const sph_params &p)
     c.h_f = p.h;
     c.inv_h_f = 1.0f / p.h;
     c.h_d = (double) p.h;
+    // the step grid's cells are h / cell_mult wide: its hash scales the float reciprocal and the
+    // double divisor by the (power-of-two) multiple, both exactly
+    c.inv_cell_f = c.inv_h_f * (float) cell_mult;
+    c.cell_d = c.h_d / (double) cell_mult;
     return c;
 }
 
+// The scenes' descriptors on the device, in the step grid of the current cell multiple m: m
+// times the reference resolution per axis, scenes' cell ranges consecutive.
 int upload_scenes(sph_ctx *c)
 {
     std::vector<SceneDev> sd(c->sc.size());
     uint32_t ob = 0;
+    const int m = c->tune.cell_mult;
+    uint64_t base = 0;
     for (size_t s = 0; s < c->sc.size(); s++) {
         const SceneHost &h = c->sc[s];
         SceneDev &d = sd[s];
         std::memset(&d, 0, sizeof(d));
         for (int a = 0; a < 3; a++) {
             d.half[a] = h.box[a] / 2.0f;
-            d.res[a] = h.res[a];
+            d.res[a] = h.res[a] * m;
             d.gravity[a] = h.gravity[a];
         }
-        d.cell_base = h.cell_base;
-        d.ncells = h.ncells;
+        d.cell_base = (uint32_t) base;
+        d.ncells = (uint32_t) ((uint64_t) d.res[0] * d.res[1] * d.res[2]);
+        base += d.ncells;
         d.obs_base = ob;
         d.n_obs = (uint32_t) h.obs.size();
         ob += d.n_obs;
     }
+    c->ctot = base;
     CK(c, cudaMemcpyAsync(c->b.scenes, sd.data(), sd.size() * sizeof(SceneDev), cudaMemcpyHostToDevice, c->stream));
     if (ob) {
         std::vector<ObstacleDev> all;
@@ -227,7 +239,7 @@ size_t pool_layout(sph_ctx *c, std::vector<PoolItem> &items)
 {
     const size_t r4 = r4_bytes(c), rs = is_f64(c) ? 8 : 4;
     const bool mixed = is_mixed(c);
-    const uint64_t N = c->ncap, C = c->ctot;
+    const uint64_t N = c->ncap, C = c->ctot_cap;
     const uint64_t nb = (C + kScanTile - 1) / kScanTile + 1;
     uint64_t nobs = 0;
     for (auto &h : c->sc) nobs += h.obs.size();
@@ -238,22 +250,22 @@ size_t pool_layout(sph_ctx *c, std::vector<PoolItem> &items)
         {&b.acc, rec ? r4 * N : 0},
         {(void **) &b.cid_u, 8 * N}, {(void **) &b.tmp, 4 * N},
         {(void **) &b.count, 4 * C}, {(void **) &b.start, 4 * (C + 1)}, {(void **) &b.cursor, 4 * C},
-        {(void **) &b.bsum, 4 * nb},
+        {(void **) &b.bsum, 4 * nb}, {(void **) &b.big, 4 * big_words(N)},
         {(void **) &b.scenes, sizeof(SceneDev) * c->sc.size()},
         {(void **) &b.obstacles, sizeof(ObstacleDev) * (nobs ? nobs : 1)},
-        {(void **) &b.scene_off, 4 * (c->sc.size() + 1)}, {(void **) &b.err, 16},
+        {(void **) &b.scene_off, 4 * (c->sc.size() + 1)}, {(void **) &b.err, 16}, {(void **) &b.tiles, 16},
         {(void **) &b.st_xyz, 12 * N}, {(void **) &b.st_vel, 12 * N},
         {(void **) &b.st_rho, rs == 4 ? 4 * N : 0}, {(void **) &b.st_p, rs == 4 ? 4 * N : 0},
         {(void **) &b.st_acc, rs == 4 && rec ? 12 * N : 0},
         {(void **) &b.st_xyz64, (rs == 8 || mixed) ? 24 * N : 0}, {(void **) &b.st_vel64, (rs == 8 || mixed) ? 24 * N : 0},
         {(void **) &b.st_rho64, (rs == 8 || mixed) ? 8 * N : 0}, {(void **) &b.st_p64, (rs == 8 || mixed) ? 8 * N : 0},
         {&b.lo_s, mixed ? 16 * N : 0}, {&b.lo_u, mixed ? 16 * N : 0},
-        {(void **) &b.gpos, mixed ? 8 * N : 0}, {(void **) &b.gvel, mixed ? 8 * N : 0},
+        {(void **) &b.gpos, mixed ? 8 * N : 0},
         {(void **) &b.st_acc64, (rs == 8 || mixed) && rec ? 24 * N : 0},
         {(void **) &b.stats, 64 * c->sc.size()},
         {(void **) &b.stats_partial, 6 * 8 * 64 * c->sc.size()},
         {(void **) &b.masks, 4 * 36 * N},
-        {(void **) &b.frec, mixed ? 0 : 2 * r4 * N},
+        {(void **) &b.frec, mixed ? 16 * N : 2 * r4 * N},
         {(void **) &b.inv, 4 * N},
     };
     size_t total = 0;
@@ -274,7 +286,7 @@ int allocate(sph_ctx *c)
     std::vector<PoolItem> items;
     const size_t total = pool_layout(c, items);
     DevBufs &b = c->b;
-    const uint64_t N = c->ncap, C = c->ctot;
+    const uint64_t N = c->ncap, C = c->ctot_cap;
     const size_t r4 = r4_bytes(c);
     cudaError_t e = cudaMalloc(&c->pool, total);
     if (e != cudaSuccess) {
@@ -302,6 +314,18 @@ int allocate(sph_ctx *c)
 // the all-pairs form is O(n^2) per scene: a check for small scenes, not a production path
 constexpr uint32_t kAllPairsMax = 131072;
 
+// Cell multiples: 1 (the reference's cells of size h) or 2 (cells of h/2 with a 5-cell stencil per
+// axis), for the plain FP32 and mixed forms' grid passes. The FP64 form (the reference run) and the
+// all-pairs form stay on the reference's grid.
+constexpr int kMaxCellMult = 2;
+bool cell_mult_allowed(const sph_ctx *c, int m, uint64_t ctot_ref)
+{
+    if (m == 1) return true;
+    if (m != 2) return false;
+    if (c->prm.precision == SPH_F64 || (c->prm.flags & SPH_FLAG_ALL_PAIRS)) return false;
+    return (uint64_t) m * m * m * ctot_ref < (1ull << 31);
+}
+
 // Validates the parameters and scenes and fills the host side of a context (scenes, cells,
 // capacity, tune); no CUDA call. Errors are reported as create errors (sph_last_error(NULL)).
 int parse_config(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *scenes, sph_ctx *c)
@@ -319,6 +343,10 @@ int parse_config(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *s
             return fail(nullptr, SPH_ERR_CAPACITY, "scene " + std::to_string(s) + ": the all-pairs form takes at most " +
                                                        std::to_string(kAllPairsMax) + " particles per scene");
     c->prm = *p;
+    if (p->precision == SPH_MIXED) {  // the mixed form's own launch forms
+        c->tune.density_p = 0;
+        c->tune.forces_mode = 0;
+    }
     if (all_pairs) {  // both passes over every particle of the scene; no variants to choose
         c->tune.density_p = Tune::ALL_PAIRS;
         c->tune.forces_mode = Tune::ALL_PAIRS;
@@ -358,6 +386,9 @@ int parse_config(const sph_params *p, uint32_t n_scenes, const sph_scene_desc *s
     if (ctot >= (1ull << 31) || ncap >= (1ull << 31) || ncap == 0)
         return fail(nullptr, SPH_ERR_ARG, "total cells and particle capacity must be in [1, 2^31)");
     c->ctot = ctot;
+    c->ctot_ref = ctot;
+    // room for the grid of cells h/2 where this form can use it (plain FP32 and mixed grid forms)
+    c->ctot_cap = cell_mult_allowed(c, 2, ctot) ? kMaxCellMult * kMaxCellMult * kMaxCellMult * ctot : ctot;
     c->ncap = ncap;
     return SPH_OK;
 }
@@ -418,7 +449,7 @@ int run_grid(sph_ctx *c)
     CK(c, Launch<R>::scan(c->b, (uint32_t) c->ctot, c->stream));
     if (is_mixed(c)) {
         CK(c, launch_slot(c->b, c->n, c->stream));
-        CK(c, mixed_permute(c->b, c->n, make_consts<float>(c->prm), make_mix(c->prm), c->stream));
+        CK(c, mixed_permute(c->b, c->n, make_consts<float>(c->prm, c->tune.cell_mult), make_mix(c->prm), c->stream));
     } else {
         CK(c, Launch<R>::permute(c->b, c->n, c->stream));
     }
@@ -427,16 +458,20 @@ int run_grid(sph_ctx *c)
 template <class R>
 int run_density(sph_ctx *c)
 {
-    if (is_mixed(c)) CK(c, mixed_density(c->b, c->n, make_consts<float>(c->prm), make_mix(c->prm), c->stream));
-    else CK(c, Launch<R>::density(c->b, c->n, make_consts<R>(c->prm), c->tune, c->stream));
+    if (is_mixed(c))
+        CK(c, mixed_density(c->b, c->n, make_consts<float>(c->prm, c->tune.cell_mult), make_mix(c->prm),
+                            c->tune.cell_mult, c->stream));
+    else CK(c, Launch<R>::density(c->b, c->n, make_consts<R>(c->prm, c->tune.cell_mult), c->tune, c->stream));
     return SPH_OK;
 }
 template <class R>
 int run_forces(sph_ctx *c)
 {
     const bool rec = (c->prm.flags & SPH_FLAG_RECORD_ACC) != 0;
-    if (is_mixed(c)) CK(c, mixed_forces(c->b, c->n, make_consts<float>(c->prm), make_mix(c->prm), rec, c->stream));
-    else CK(c, Launch<R>::forces(c->b, c->n, make_consts<R>(c->prm), rec, c->tune, c->stream));
+    if (is_mixed(c))
+        CK(c, mixed_forces(c->b, c->n, make_consts<float>(c->prm, c->tune.cell_mult), make_mix(c->prm), rec,
+                           c->tune.forces_mode, c->tune.cell_mult, c->stream));
+    else CK(c, Launch<R>::forces(c->b, c->n, make_consts<R>(c->prm, c->tune.cell_mult), rec, c->tune, c->stream));
     return SPH_OK;
 }
 
@@ -520,11 +555,18 @@ float elapsed(cudaEvent_t a, cudaEvent_t b)
 // timed from the start of its grid pass to the end of its force pass; the fastest is kept
 // until the next trial. A trial step waits for its own end (one host synchronisation per
 // candidate).
+// The mixed form's candidates are its four launch forms (blocks of 128 or 256 threads, with and
+// without a 48-register cap).
 constexpr int kOnlineCand[kOnlineN] = {7, 9, 10, 11};
+constexpr int kOnlineCandMixed[kOnlineN] = {0, 1, 2, 3};
+static_assert(kOnlineN == kMixedVariants, "every mixed variant is an online candidate");
+
+int online_candidate(const sph_ctx *c, int k) { return is_mixed(c) ? kOnlineCandMixed[k] : kOnlineCand[k]; }
 
 bool online_active(const sph_ctx *c)
 {
-    return c->online_period > 0 && !is_mixed(c) && c->tune.forces_mode >= 3 && c->tune.forces_mode <= 11;
+    if (c->online_period <= 0) return false;
+    return is_mixed(c) || (c->tune.forces_mode >= 3 && c->tune.forces_mode <= 12);
 }
 
 // before a step: start a due trial and set this step's candidate
@@ -533,7 +575,7 @@ int online_begin_step(sph_ctx *c)
     if (!online_active(c)) return SPH_OK;
     if (c->trial < 0 && c->steps_run % (uint64_t) c->online_period == 0) c->trial = 0;
     if (c->trial < 0) return SPH_OK;
-    c->tune.forces_mode = kOnlineCand[c->trial];
+    c->tune.forces_mode = online_candidate(c, c->trial);
     CK(c, cudaEventRecord(c->on_ev[0], c->stream));
     return SPH_OK;
 }
@@ -550,13 +592,21 @@ int online_end_step(sph_ctx *c)
     int best = 0;
     for (int k = 1; k < kOnlineN; k++)
         if (c->trial_ms[k] < c->trial_ms[best]) best = k;
-    c->tune.forces_mode = kOnlineCand[best];
+    c->tune.forces_mode = online_candidate(c, best);
     c->trial = -1;
     return SPH_OK;
 }
 
 bool valid_density(int v) { return v == 0 || v == 1 || v == 2 || v == 4; }
-bool valid_forces(int v) { return v >= 0 && v <= 11; }
+bool valid_forces(int v) { return v >= 0 && v <= 12; }
+// the mixed form has its own force variants and one density pass (density variant 0); cells of
+// h/2 run the plain form's record variants 7 to 11
+bool valid_variant(const sph_ctx *c, int dv, int fv, int cell_mult)
+{
+    if (is_mixed(c)) return dv == 0 && fv >= 0 && fv < kMixedVariants;
+    if (cell_mult == 2) return dv == 0 && fv >= 7 && fv <= 11;
+    return valid_density(dv) && valid_forces(fv);
+}
 
 int bucket_of(uint64_t n)
 {
@@ -584,8 +634,9 @@ std::string tune_key(const sph_ctx *c, uint64_t n)
     return dev + "|p" + std::to_string(c->prm.precision) + "|b" + std::to_string(bucket_of(n));
 }
 
-// cached (density, forces) variants for key, if any
-bool tune_lookup(const std::string &key, int &dv, int &fv)
+// cached (density, forces, cell multiple) choice for key, if any; lines are "key d f m" (a line
+// without m is cell multiple 1)
+bool tune_lookup(const sph_ctx *c, const std::string &key, int &dv, int &fv, int &mv)
 {
     std::ifstream f(tune_cache_path());
     std::string line;
@@ -593,25 +644,65 @@ bool tune_lookup(const std::string &key, int &dv, int &fv)
     while (std::getline(f, line)) {
         std::istringstream is(line);
         std::string k;
-        int d, fo;
-        if (is >> k >> d >> fo && k == key && valid_density(d) && valid_forces(fo)) {
+        int d, fo, m = 1;
+        if (!(is >> k >> d >> fo) || k != key) continue;
+        if (!(is >> m)) m = 1;
+        if (cell_mult_allowed(c, m, c->ctot_ref) && valid_variant(c, d, fo, m)) {
             dv = d;
             fv = fo;
+            mv = m;
             found = true;  // the last entry wins
         }
     }
     return found;
 }
 
-void tune_store(const std::string &key, int dv, int fv)
+void tune_store(const std::string &key, int dv, int fv, int mv)
 {
     const std::string path = tune_cache_path();
     for (size_t p = path.find('/', 1); p != std::string::npos; p = path.find('/', p + 1))
         mkdir(path.substr(0, p).c_str(), 0755);
     std::ofstream f(path, std::ios::app);
-    if (f) f << key << " " << dv << " " << fv << "\n";
+    if (f) f << key << " " << dv << " " << fv << " " << mv << "\n";
 }
 
+
+// Switches the step grid to cells of h / m: the scenes' descriptors, the counts, and the cell of
+// every held particle (the *_u arrays) in the new grid. Only between steps. Cells of h/2 run the
+// record variants of the plain form (7 to 11); another plain variant becomes 10.
+int set_cell_mult(sph_ctx *c, int m)
+{
+    if (m == c->tune.cell_mult) return SPH_OK;
+    drop_graph(c);
+    c->tune.cell_mult = m;
+    if (m == 2 && !is_mixed(c) && c->tune.forces_mode < 7) {
+        c->tune.density_p = 0;
+        c->tune.forces_mode = 10;
+    }
+    int rc = upload_scenes(c);  // also sets c->ctot
+    if (rc) return rc;
+    CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
+    if (c->state == HASHED && c->n) {
+        if (is_f64(c)) CK(c, Launch<double>::rehash(c->b, c->n, make_consts<double>(c->prm, m), c->stream));
+        else CK(c, Launch<float>::rehash(c->b, c->n, make_consts<float>(c->prm, m), c->stream));
+    }
+    return SPH_OK;
+}
+
+// After a grid pass: the unsorted arrays refilled from the sorted state (the trial force passes
+// of the autotuner overwrite them), hashed again, ready for another grid pass of the same state.
+int refill_unsorted(sph_ctx *c)
+{
+    const size_t r4 = r4_bytes(c);
+    CK(c, cudaMemcpyAsync(c->b.pos_u, c->b.pos_s, r4 * c->n, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->b.vel_u, c->b.vel_s, r4 * c->n, cudaMemcpyDeviceToDevice, c->stream));
+    if (is_mixed(c)) CK(c, cudaMemcpyAsync(c->b.lo_u, c->b.lo_s, 16ull * c->n, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
+    if (is_f64(c)) CK(c, Launch<double>::rehash(c->b, c->n, make_consts<double>(c->prm, c->tune.cell_mult), c->stream));
+    else CK(c, Launch<float>::rehash(c->b, c->n, make_consts<float>(c->prm, c->tune.cell_mult), c->stream));
+    c->state = HASHED;
+    return SPH_OK;
+}
 
 }  // namespace
 
@@ -674,6 +765,7 @@ int sph_debug_check(sph_ctx *c, uint32_t *flags)
     CK(c, check_flags_kernels(flags));
     CK(c, check_flags_mixed(flags));
     CK(c, check_flags_handoff(flags));
+    CK(c, check_flags_noalloc(flags));
     std::vector<unsigned char> buf(kCanaryBytes);
     for (unsigned char *g : c->canaries) {
         CK(c, cudaMemcpy(buf.data(), g, kCanaryBytes, cudaMemcpyDeviceToHost));
@@ -744,6 +836,15 @@ int sph_upload(sph_ctx *c, const float *xyz, const float *vel, const uint32_t *c
         drop_graph(c);
         for (size_t s = 0; s < c->sc.size(); s++) c->sc[s].count = counts[s];
         c->n = (uint32_t) total;
+        // the cached choice of this particle-count bucket, its cell multiple before the hash
+        int dv, fv, mv;
+        if (!c->tune_pinned && tune_lookup(c, tune_key(c, total), dv, fv, mv)) {
+            c->state = EMPTY;
+            int rc = set_cell_mult(c, mv);
+            if (rc) return rc;
+            c->tune.density_p = dv;
+            c->tune.forces_mode = fv;
+        }
         int rc = upload_scene_off(c);
         if (rc) return rc;
         CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
@@ -760,15 +861,10 @@ int sph_upload(sph_ctx *c, const float *xyz, const float *vel, const uint32_t *c
             }
             if (is_f64(c))
                 CK(c, Launch<double>::ingest(c->b, sx, sv, 0, c->n, -1, 0, (uint32_t) c->sc.size(),
-                                             make_consts<double>(c->prm), c->stream));
+                                             make_consts<double>(c->prm, c->tune.cell_mult), c->stream));
             else
                 CK(c, Launch<float>::ingest(c->b, sx, sv, 0, c->n, -1, 0, (uint32_t) c->sc.size(),
-                                            make_consts<float>(c->prm), c->stream));
-        }
-        int dv, fv;
-        if (!c->tune_pinned && tune_lookup(tune_key(c, total), dv, fv)) {
-            c->tune.density_p = dv;
-            c->tune.forces_mode = fv;
+                                            make_consts<float>(c->prm, c->tune.cell_mult), c->stream));
         }
         c->state = HASHED;
         c->n_sorted = 0;
@@ -802,10 +898,10 @@ int append_ingest(sph_ctx *c, uint32_t scene, uint32_t n, bool has_vel)
     if (is_mixed(c)) CK(c, cudaMemsetAsync((char *) c->b.lo_u + 16ull * c->n, 0, 16ull * n, c->stream));
     if (is_f64(c))
         CK(c, Launch<double>::ingest(c->b, c->b.st_xyz, has_vel ? c->b.st_vel : nullptr, c->n, n, (int32_t) scene,
-                                     h.count, (uint32_t) c->sc.size(), make_consts<double>(c->prm), c->stream));
+                                     h.count, (uint32_t) c->sc.size(), make_consts<double>(c->prm, c->tune.cell_mult), c->stream));
     else
         CK(c, Launch<float>::ingest(c->b, c->b.st_xyz, has_vel ? c->b.st_vel : nullptr, c->n, n, (int32_t) scene,
-                                    h.count, (uint32_t) c->sc.size(), make_consts<float>(c->prm), c->stream));
+                                    h.count, (uint32_t) c->sc.size(), make_consts<float>(c->prm, c->tune.cell_mult), c->stream));
     h.count += n;
     c->n += n;
     c->appended = true;
@@ -855,8 +951,10 @@ int sph_set_gravity(sph_ctx *c, int32_t scene, const float g[3])
     return upload_scenes(c);
 }
 
-// Pass-by-pass calls; with SPH_FLAG_PROFILE each records CUDA events around its work and
-// the force pass resolves the three times (sProfilingEvent's grid, density, forces fields).
+// Pass-by-pass calls. With SPH_FLAG_PROFILE each records CUDA events around its work and waits
+// for its own end, so that its time (sProfilingEvent's grid, density or forces field) is known
+// when the call returns, as each pass of the reference returns its own profiled duration
+// (src/CBaseParticleSimulator.cpp:116-144).
 int sph_pass_grid(sph_ctx *c)
 {
     if (!c) return SPH_ERR_ARG;
@@ -866,7 +964,11 @@ int sph_pass_grid(sph_ctx *c)
     if (rc) return rc;
     if (prof) CK(c, cudaEventRecord(c->ev[0], c->stream));
     rc = pass_grid(c);
-    if (!rc && prof) CK(c, cudaEventRecord(c->ev[1], c->stream));
+    if (!rc && prof) {
+        CK(c, cudaEventRecord(c->ev[1], c->stream));
+        CK(c, cudaEventSynchronize(c->ev[1]));
+        c->ms[0] = elapsed(c->ev[0], c->ev[1]);
+    }
     return rc;
 }
 int sph_pass_density(sph_ctx *c)
@@ -874,7 +976,11 @@ int sph_pass_density(sph_ctx *c)
     if (!c) return SPH_ERR_ARG;
     CK(c, cudaSetDevice(c->device));
     int rc = pass_density(c);
-    if (!rc && (c->prm.flags & SPH_FLAG_PROFILE)) CK(c, cudaEventRecord(c->ev[2], c->stream));
+    if (!rc && (c->prm.flags & SPH_FLAG_PROFILE)) {
+        CK(c, cudaEventRecord(c->ev[2], c->stream));
+        CK(c, cudaEventSynchronize(c->ev[2]));
+        c->ms[1] = elapsed(c->ev[1], c->ev[2]);
+    }
     return rc;
 }
 int sph_pass_forces(sph_ctx *c)
@@ -885,8 +991,6 @@ int sph_pass_forces(sph_ctx *c)
     if (!rc && (c->prm.flags & SPH_FLAG_PROFILE)) {
         CK(c, cudaEventRecord(c->ev[3], c->stream));
         CK(c, cudaEventSynchronize(c->ev[3]));
-        c->ms[0] = elapsed(c->ev[0], c->ev[1]);
-        c->ms[1] = elapsed(c->ev[1], c->ev[2]);
         c->ms[2] = elapsed(c->ev[2], c->ev[3]);
         c->ms[3] = 0;
         c->ms[4] = 0;
@@ -970,7 +1074,7 @@ int sph_set_online_tuning(sph_ctx *c, int32_t period)
 {
     if (!c) return SPH_ERR_ARG;
     if (period != 0 && period < kOnlineN) return fail(c, SPH_ERR_ARG, "period must be 0 (off) or at least 4 steps");
-    if (period && (is_mixed(c) || (c->prm.flags & SPH_FLAG_ALL_PAIRS)))
+    if (period && (c->prm.flags & SPH_FLAG_ALL_PAIRS))
         return fail(c, SPH_ERR_STATE, "this context has no force variants to tune");
     if (c->trial >= 0) return fail(c, SPH_ERR_STATE, "a tuning trial is in progress");
     CK(c, cudaSetDevice(c->device));
@@ -984,8 +1088,10 @@ int sph_set_variant(sph_ctx *c, int32_t density_variant, int32_t forces_variant)
 {
     if (!c) return SPH_ERR_ARG;
     if (c->prm.flags & SPH_FLAG_ALL_PAIRS) return fail(c, SPH_ERR_STATE, "an all-pairs context has no launch variants");
-    if (!valid_density(density_variant) || !valid_forces(forces_variant))
-        return fail(c, SPH_ERR_ARG, "unknown launch variant");
+    if (!valid_variant(c, density_variant, forces_variant, c->tune.cell_mult))
+        return fail(c, SPH_ERR_ARG, is_mixed(c) ? "unknown launch variant (mixed form: density 0, forces 0-3)"
+                                    : c->tune.cell_mult == 2 ? "unknown launch variant (cells of h/2: density 0, forces 7-11)"
+                                                             : "unknown launch variant");
     c->tune.density_p = density_variant;
     c->tune.forces_mode = forces_variant;
     c->tune_pinned = true;
@@ -1010,59 +1116,98 @@ int sph_autotune(sph_ctx *c, int32_t reps)
     if (c->n == 0) return fail(c, SPH_ERR_STATE, "autotune needs particles");
     CK(c, cudaSetDevice(c->device));
     drop_graph(c);
-    if (is_mixed(c)) return one_step(c);  // one launch form: nothing to choose
-    int rc = pass_grid(c);
-    if (rc) return rc;
-    // every (density, forces) pair, timed as density + forces on the same sorted state; the
-    // mask-driven force pass (3) brings its own density pass
+    // every (cell multiple, density, forces) choice on the same state: per cell multiple the grid
+    // pass once, then each (density, forces) pair timed as density + forces on its sorted state;
+    // the choice minimises grid + density + forces. Between cell multiples the unsorted arrays are
+    // refilled from the sorted starting state (the trials' force passes overwrote them).
     struct Cfg { int d, f; };
-    std::vector<Cfg> cfgs;
-    for (int d : {0, 1, 2, 4})
-        for (int f = 0; f <= 2; f++) cfgs.push_back({d, f});
-    cfgs.push_back({0, 3});
-    cfgs.push_back({0, 4});
-    cfgs.push_back({0, 5});
-    cfgs.push_back({0, 6});
-    cfgs.push_back({0, 7});
-    cfgs.push_back({0, 8});
-    cfgs.push_back({0, 9});
-    cfgs.push_back({0, 10});
-    cfgs.push_back({0, 11});
     float best = 1e30f;
-    int bd = c->tune.density_p, bf = c->tune.forces_mode;
-    for (const Cfg &g : cfgs) {
-        c->tune.density_p = g.d;
-        c->tune.forces_mode = g.f;
-        for (int r = 0; r <= reps; r++) {  // the first run is a warm-up
-            CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));  // the force pass adds to the counts
-            CK(c, cudaEventRecord(c->ev[0], c->stream));
-            c->state = SORTED;
-            rc = pass_density(c);
-            if (!rc) rc = pass_forces(c);
+    int bm = c->tune.cell_mult, bd = c->tune.density_p, bf = c->tune.forces_mode;
+    std::vector<int> mults = {1};
+    if (cell_mult_allowed(c, 2, c->ctot_ref)) mults.push_back(2);
+    for (size_t mi = 0; mi < mults.size(); mi++) {
+        const int m = mults[mi];
+        if (mi > 0) {
+            int rc = refill_unsorted(c);
+            if (!rc) rc = set_cell_mult(c, m);
             if (rc) return rc;
-            CK(c, cudaEventRecord(c->ev[1], c->stream));
-            CK(c, cudaEventSynchronize(c->ev[1]));
-            const float ms = elapsed(c->ev[0], c->ev[1]);
-            if (r > 0 && ms < best) {
-                best = ms;
-                bd = g.d;
-                bf = g.f;
+        } else if (m != c->tune.cell_mult) {
+            int rc = set_cell_mult(c, m);
+            if (rc) return rc;
+        }
+        CK(c, cudaEventRecord(c->ev[0], c->stream));
+        int rc = pass_grid(c);
+        if (rc) return rc;
+        CK(c, cudaEventRecord(c->ev[1], c->stream));
+        CK(c, cudaEventSynchronize(c->ev[1]));
+        const float grid_ms = elapsed(c->ev[0], c->ev[1]);
+        std::vector<Cfg> cfgs;
+        if (is_mixed(c)) {
+            for (int f = 0; f < kMixedVariants; f++) cfgs.push_back({0, f});
+        } else if (m == 2) {
+            for (int f = 7; f <= 11; f++) cfgs.push_back({0, f});
+        } else {
+            for (int d : {0, 1, 2, 4})
+                for (int f = 0; f <= 2; f++) cfgs.push_back({d, f});
+            for (int f = 3; f <= 12; f++) cfgs.push_back({0, f});
+        }
+        for (const Cfg &g : cfgs) {
+            c->tune.density_p = g.d;
+            c->tune.forces_mode = g.f;
+            for (int r = 0; r <= reps; r++) {  // the first run is a warm-up
+                CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));  // the force pass adds to the counts
+                CK(c, cudaEventRecord(c->ev[0], c->stream));
+                c->state = SORTED;
+                rc = pass_density(c);
+                if (!rc) rc = pass_forces(c);
+                if (rc) return rc;
+                CK(c, cudaEventRecord(c->ev[1], c->stream));
+                CK(c, cudaEventSynchronize(c->ev[1]));
+                const float ms = grid_ms + elapsed(c->ev[0], c->ev[1]);
+                if (r > 0 && ms < best) {
+                    best = ms;
+                    bm = m;
+                    bd = g.d;
+                    bf = g.f;
+                }
             }
         }
     }
-    // the step itself, with the chosen variants (every variant computes the same bits)
+    // the step itself, with the chosen cell multiple and variants, from the starting state
+    if (bm != c->tune.cell_mult) {
+        int rc = refill_unsorted(c);
+        if (!rc) rc = set_cell_mult(c, bm);
+        if (!rc) rc = pass_grid(c);
+        if (rc) return rc;
+    }
     c->tune.density_p = bd;
     c->tune.forces_mode = bf;
     CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
     c->state = SORTED;
-    rc = pass_density(c);
+    int rc = pass_density(c);
     if (!rc) rc = pass_forces(c);
     if (rc) return rc;
     c->tune_pinned = true;
     c->steps_run++;  // the step above was a real one
-    tune_store(tune_key(c, c->n), bd, bf);
+    tune_store(tune_key(c, c->n), bd, bf, bm);
     return SPH_OK;
 }
+
+int sph_set_cell_multiple(sph_ctx *c, int32_t m)
+{
+    if (!c) return SPH_ERR_ARG;
+    if (m != 1 && m != 2) return fail(c, SPH_ERR_ARG, "the cell multiple is 1 (cells of h) or 2 (cells of h/2)");
+    if (!cell_mult_allowed(c, m, c->ctot_ref))
+        return fail(c, SPH_ERR_UNSUPPORTED, "cells of h/2 are for the plain FP32 and mixed grid forms");
+    if (c->state != HASHED && c->state != EMPTY)
+        return fail(c, SPH_ERR_STATE, "the cell multiple changes between steps (not between passes)");
+    CK(c, cudaSetDevice(c->device));
+    const int rc = set_cell_mult(c, m);
+    if (!rc) c->tune_pinned = true;
+    return rc;
+}
+
+int sph_get_cell_multiple(const sph_ctx *c) { return c ? c->tune.cell_mult : SPH_ERR_ARG; }
 
 int sph_pass_times(sph_ctx *c, double ms[5])
 {
@@ -1294,12 +1439,71 @@ int sph_download_f64(sph_ctx *c, double *xyz, double *vel, double *rho, double *
     }
 }
 
+namespace {
+
+// The reference's grid (cells of size h) of the current sorted state when the step runs on cells
+// of h/2: per scene, the id-ordered positions go through the same grid build as
+// sph_grid_build_noalloc, with working memory allocated for the call.
+int get_grid_ref(sph_ctx *c, uint32_t *cell_of_particle, uint32_t *cell_counts, uint32_t *sorted_ids)
+{
+    const uint32_t n = c->n;
+    // id-ordered float positions of the sorted state (the mixed form's hi part: its hash input)
+    if (is_mixed(c)) CK(c, mixed_egress(c->b, n, 0, 0, 1, 1, false, c->stream));
+    else CK(c, Launch<float>::egress(c->b, n, 0, 0, 1, 1, c->stream));
+    uint64_t nmax = 1, cmax = 1;
+    for (auto &h : c->sc) {
+        nmax = std::max<uint64_t>(nmax, h.count);
+        cmax = std::max<uint64_t>(cmax, (uint64_t) h.res[0] * h.res[1] * h.res[2]);
+    }
+    const uint64_t nb = cmax / kScanTile + 1;
+    const uint64_t words = nmax + (cmax + 1) + nmax + 2 * cmax + nmax + nb + big_words(nmax);
+    uint32_t *mem = nullptr;
+    CK(c, cudaMalloc(&mem, 4 * words));
+    uint32_t *d_cell = mem, *d_start = d_cell + nmax, *d_order = d_start + cmax + 1;
+    GridScratch g;
+    g.count = d_order + nmax;
+    g.cursor = g.count + cmax;
+    g.tmp = g.cursor + cmax;
+    g.bsum = g.tmp + nmax;
+    g.big = g.bsum + nb;
+    uint64_t off = 0, cbase = 0;
+    cudaError_t e = cudaSuccess;
+    std::vector<uint32_t> cell, start, order;
+    for (size_t s = 0; s < c->sc.size() && e == cudaSuccess; s++) {
+        const SceneHost &h = c->sc[s];
+        const uint64_t nc = (uint64_t) h.res[0] * h.res[1] * h.res[2];
+        const int3 res = make_int3(h.res[0], h.res[1], h.res[2]);
+        const float3 half = make_float3(h.box[0] / 2.0f, h.box[1] / 2.0f, h.box[2] / 2.0f);
+        e = ref_grid_build(c->b.st_xyz + 3 * off, h.count, res, half, c->prm.h, d_cell, d_start, d_order, g, c->stream);
+        cell.resize(h.count);
+        order.resize(h.count);
+        start.resize(nc + 1);
+        if (e == cudaSuccess && h.count) e = cudaMemcpyAsync(cell.data(), d_cell, 4ull * h.count, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess && h.count) e = cudaMemcpyAsync(order.data(), d_order, 4ull * h.count, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(start.data(), d_start, 4 * (nc + 1), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) break;
+        if (cell_of_particle) std::memcpy(cell_of_particle + off, cell.data(), 4ull * h.count);
+        if (sorted_ids) std::memcpy(sorted_ids + off, order.data(), 4ull * h.count);
+        if (cell_counts)
+            for (uint64_t k = 0; k < nc; k++) cell_counts[cbase + k] = start[k + 1] - start[k];
+        off += h.count;
+        cbase += nc;
+    }
+    cudaFree(mem);
+    if (e != cudaSuccess) return cuda_fail(c, e, "reference grid of the sorted state");
+    return SPH_OK;
+}
+
+}  // namespace
+
 int sph_get_grid(sph_ctx *c, uint32_t *cell_of_particle, uint32_t *cell_counts, uint32_t *sorted_ids)
 {
     if (!c) return SPH_ERR_ARG;
     if (c->state != SORTED && c->state != DENSE) return fail(c, SPH_ERR_STATE, "the grid is available after a grid pass");
     try {
         CK(c, cudaSetDevice(c->device));
+        if (c->tune.cell_mult != 1) return get_grid_ref(c, cell_of_particle, cell_counts, sorted_ids);
         const uint32_t n = c->n;
         std::vector<uint32_t> start(c->ctot + 1);
         CK(c, cudaMemcpyAsync(start.data(), c->b.start, 4 * (c->ctot + 1), cudaMemcpyDeviceToHost, c->stream));
@@ -1346,8 +1550,8 @@ int sph_stats(sph_ctx *c, uint32_t scene, double out[8])
         return fail(c, SPH_ERR_STATE, "statistics need a completed step or a density pass");
     CK(c, cudaSetDevice(c->device));
     const int layout_sorted = c->state == DENSE ? 1 : 0;
-    if (is_f64(c)) CK(c, Launch<double>::stats(c->b, (uint32_t) c->sc.size(), make_consts<double>(c->prm), layout_sorted, c->stream));
-    else CK(c, Launch<float>::stats(c->b, (uint32_t) c->sc.size(), make_consts<float>(c->prm), layout_sorted, c->stream));
+    if (is_f64(c)) CK(c, Launch<double>::stats(c->b, (uint32_t) c->sc.size(), make_consts<double>(c->prm, c->tune.cell_mult), layout_sorted, c->stream));
+    else CK(c, Launch<float>::stats(c->b, (uint32_t) c->sc.size(), make_consts<float>(c->prm, c->tune.cell_mult), layout_sorted, c->stream));
     CK(c, cudaMemcpyAsync(out, c->b.stats + 8 * scene, 64, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     return SPH_OK;

@@ -117,15 +117,34 @@ __device__ __forceinline__ double rfma(double a, double b, double c) { return __
 __device__ __forceinline__ float inv_sqrt(float x) { return rsqrtf(x); }
 __device__ __forceinline__ double inv_sqrt(double x) { return 1.0 / sqrt(x); }
 
+// The cell of a position in the step grid (cells h / cell multiple wide), and its global index.
 template <class R>
 __device__ __forceinline__ uint32_t hash_cell(const SceneDev &sc, R x, R y, R z, const Consts<R> &c, int &cx,
                                               int &cy, int &cz)
 {
-    cx = cell_axis(x, sc.half[0], c.inv_h_f, c.h_d, sc.res[0]);
-    cy = cell_axis(y, sc.half[1], c.inv_h_f, c.h_d, sc.res[1]);
-    cz = cell_axis(z, sc.half[2], c.inv_h_f, c.h_d, sc.res[2]);
+    cx = cell_axis(x, sc.half[0], c.inv_cell_f, c.cell_d, sc.res[0]);
+    cy = cell_axis(y, sc.half[1], c.inv_cell_f, c.cell_d, sc.res[1]);
+    cz = cell_axis(z, sc.half[2], c.inv_cell_f, c.cell_d, sc.res[2]);
     return sc.cell_base + (uint32_t) cx + (uint32_t) cy * (uint32_t) sc.res[0] +
            (uint32_t) cz * (uint32_t) sc.res[0] * (uint32_t) sc.res[1];
+}
+
+// Row r of the stencil around cell (cx, cy, cz): its candidate range [jb, je), or false if the
+// row lies outside the grid.
+template <int RAD>
+__device__ __forceinline__ bool stencil_row(const SceneDev &sc, const uint32_t *__restrict__ start, int cx, int cy,
+                                            int cz, int r, uint32_t &jb, uint32_t &je)
+{
+    const int D = 2 * RAD + 1;
+    const int dz = r / D - RAD, dy = r % D - RAD;
+    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
+    const int z = cz + dz, y = cy + dy;
+    if (z < 0 || z >= Z || y < 0 || y >= Y) return false;
+    const int xl = cx - RAD > 0 ? cx - RAD : 0, xh = cx + RAD < X ? cx + RAD : X - 1;
+    const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
+    jb = __ldg(start + row + xl);
+    je = __ldg(start + row + xh + 1);
+    return true;
 }
 
 __device__ __forceinline__ SceneDev load_scene(const SceneDev *scenes, uint32_t s)
@@ -318,7 +337,28 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
 }
 
-// Words of neighbour mask recorded per particle and row (32 candidates each).
-constexpr int MASK_WORDS = 4;
+
+// Rank of id among the ids of its cell, the slots tmp[b, e): the number of smaller ids. Cells of
+// at most kBigCell particles are counted directly (occupancy^2 work per cell, trivial at such
+// sizes). Larger cells, up to kBigCellMax, have had their slots sorted by k_sort_big, and the
+// rank is a lower-bound search. Cells above kBigCellMax (thousands of times the rest density)
+// keep the count.
+__device__ __forceinline__ uint32_t rank_in_cell(const uint32_t *__restrict__ tmp, uint32_t b, uint32_t e,
+                                                 uint32_t id)
+{
+    const uint32_t occ = e - b;
+    if (occ > kBigCell && occ <= kBigCellMax) {
+        uint32_t lo = b, hi = e;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (tmp[mid] < id) lo = mid + 1;
+            else hi = mid;
+        }
+        return lo - b;
+    }
+    uint32_t r = 0;
+    for (uint32_t k = b; k < e; k++) r += tmp[k] < id ? 1u : 0u;
+    return r;
+}
 
 }  // namespace sph

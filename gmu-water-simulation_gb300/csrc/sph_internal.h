@@ -7,8 +7,10 @@
 namespace sph {
 
 // Device-side descriptor of one scene of a batch. Cells of scene s occupy the global
-// cell range [cell_base, cell_base + ncells); a scene's grid is (int) ceil(box / h) cells
-// per axis and its linear cell index is x + y*X + z*X*Y (include/CGrid.h:25-28).
+// cell range [cell_base, cell_base + ncells) of the step's grid. With cell multiple 1 that is the
+// reference's grid: (int) ceil(box / h) cells per axis, linear index x + y*X + z*X*Y
+// (include/CGrid.h:25-28). With cell multiple m the step's cells are h/m wide and res is m times
+// the reference's resolution (the same extent, split m ways per axis).
 struct alignas(16) SceneDev {
     float half[3];      // box / 2 (exact in float), the wall positions
     uint32_t cell_base;
@@ -36,8 +38,12 @@ struct Consts {
     R dt;
     R c_poly6, c_spiky, c_visc;  // 315/(64 pi h^9), -45/(pi h^6), 45/(pi h^6)
     R wall_k, wall_damp, wall_r;
-    float h_f, inv_h_f; // float copies used by the cell hash (h as float, 1/h rounded)
-    double h_d;         // (double) h, divisor of the exact hash
+    float h_f, inv_h_f; // h as float, 1/h rounded (the mixed form's h-cell codes)
+    double h_d;         // (double) h
+    // the step grid's cell width h/m: the hash's float reciprocal (m times 1/h rounded, exactly)
+    // and the divisor of its exact double formula
+    float inv_cell_f;
+    double cell_d;
 };
 
 // Buffers of one context, in the layout of the precision form.
@@ -52,22 +58,25 @@ struct DevBufs {
     uint32_t *start;       // exclusive scan of count, ncells_total + 1 entries
     uint32_t *cursor;      // running slot per cell (starts at start[c])
     uint32_t *bsum;        // scan block sums
+    uint32_t *big;         // cells above kBigCell particles: count in word 0, then the cells (big_words(n) words)
     SceneDev *scenes;
     ObstacleDev *obstacles;
     uint32_t *scene_off;   // first output index of every scene (id-order downloads)
     int32_t *err;          // device error flag
+    uint32_t *tiles;       // tile counters of the persistent launches (density, forces), zeroed before each
     // staging for host transfers (ingest / egress)
     float *st_xyz, *st_vel, *st_rho, *st_p, *st_acc;
     double *st_xyz64, *st_vel64, *st_rho64, *st_p64, *st_acc64;
     double *stats;         // per-scene FP64 reductions, 8 doubles each
     double *stats_partial; // per-scene slices of the reductions (kSplit x 6 doubles each)
     uint32_t *masks;       // accepted-neighbour bit masks of the density pass, 36 words per particle
-    void *frec;            // force records of the density pass (variants 7-9): (x, y, z, c_spiky p/rho^2), (v, c_visc/rho)
+    void *frec;            // force records of the density pass: plain/FP64 variants 7-11 (x, y, z, c_spiky p/rho^2),
+                           // (v, c_visc/rho); mixed: one 16-byte record per particle (sph_mixed.cu)
     uint32_t *inv;         // layout index of each particle in id order (downloads into pinned host memory)
     // mixed-precision form only
     void *lo_s, *lo_u;     // low parts of the hi/lo positions (float4, .w unused)
     uint2 *gpos;           // gathered positions: 16-bit codes x | y << 16, z (sorted order)
-    uint2 *gvel;           // gathered velocities: FP16 x, y, z, 0 (sorted order)
+                           // (the mixed form's neighbour records, 16 bytes each, live in frec)
 };
 
 // ---- exact cell hash -------------------------------------------------------------
@@ -117,16 +126,41 @@ struct MixConsts {
 //               neighbour per iteration without/with a 64-register cap, 5/6 two per
 //               iteration with/without it, 7 as 6 with each neighbour's terms read from one
 //               packed force record (two 16-byte loads from one 32-byte record), 8 and 9 as
-//               7 at 48 and 40 registers, 10 and 11 as 9 and 8 in blocks of 128 threads
+//               7 at 48 and 40 registers, 10 and 11 as 9 and 8 in blocks of 128 threads; 12 = 10 with
+//               both neighbour passes as persistent launches over dynamically fetched tiles
+//   cell_mult : the step grid's cells are h / cell_mult wide (1 or 2); the neighbour passes walk
+//               (2 cell_mult + 1)^2 rows of 2 cell_mult + 1 cells (only the mask-driven record
+//               variants, 7 to 11 and the mixed form's, run on cells of h/2)
 struct Tune {
     static constexpr int ALL_PAIRS = 16;  // both passes over every particle of the scene
     int density_p = 2;
     int forces_mode = 3;
+    int cell_mult = 1;
 };
+
+// Neighbour rows of the stencil of radius RAD cells (RAD = cell multiple): (2 RAD + 1)^2 rows,
+// each 2 RAD + 1 cells along x, with WORDS mask words of 32 candidates recorded per row. The
+// mask buffer holds 36 words per particle: 9 rows x 4 words, or 25 rows x 1 word.
+template <int RAD>
+struct Stencil {
+    static constexpr int ROWS = (2 * RAD + 1) * (2 * RAD + 1);
+    static constexpr int WORDS = RAD == 1 ? 4 : 1;
+    static_assert(ROWS * WORDS <= 36, "the masks fit the per-particle mask buffer");
+};
+constexpr int kMaskWordsPerParticle = 36;
 
 // Cells per block of the cell-count scan; the block-sum buffer holds one word per tile
 // (plus one) and is sized with this constant wherever it is allocated.
 constexpr uint32_t kScanTile = 1024;
+
+// Cells holding more than kBigCell particles are listed by the scan and their slot ids sorted
+// (k_sort_big), so that the canonical rank is a search instead of an occupancy^2 count (cells up
+// to kBigCell, 16 times the rest occupancy, are counted directly: at most 128 loads a particle).
+// Sorting happens in shared memory for cells of up to kBigCellMax particles. The list holds its
+// length in word 0 and at most n / kBigCell cells: big_words(n) words.
+constexpr uint32_t kBigCell = 128;
+constexpr uint32_t kBigCellMax = 4096;
+__host__ __device__ constexpr uint64_t big_words(uint64_t n) { return n / kBigCell + 2; }
 
 // ---- kernel launchers (sph_kernels.cu) --------------------------------------------
 template <class R>
@@ -138,6 +172,9 @@ struct Launch {
                               int32_t scene, uint32_t id0, uint32_t nscenes, Consts<R> c, cudaStream_t st);
     static cudaError_t scan(const DevBufs &b, uint32_t ncells, cudaStream_t st);
     static cudaError_t permute(const DevBufs &b, uint32_t n, cudaStream_t st);
+    // positions of the first n *_u particles hashed again into the step grid (after the cell
+    // multiple changed): counts and the cells of cid_u
+    static cudaError_t rehash(const DevBufs &b, uint32_t n, Consts<R> c, cudaStream_t st);
     static cudaError_t density(const DevBufs &b, uint32_t n, Consts<R> c, const Tune &t, cudaStream_t st);
     static cudaError_t forces(const DevBufs &b, uint32_t n, Consts<R> c, bool record_acc, const Tune &t,
                               cudaStream_t st);
@@ -150,6 +187,9 @@ struct Launch {
 
 // slot assignment of the counting sort alone (the mixed form has its own permute)
 cudaError_t launch_slot(const DevBufs &b, uint32_t n, cudaStream_t st);
+
+// sorts the slot ids of every cell the scan listed in big (after the slots are taken)
+cudaError_t launch_sort_big(const uint32_t *start, uint32_t *tmp, const uint32_t *big, cudaStream_t st);
 
 // disc emitter on the device (sph_emit.cu): n particles into the float3 staging arrays
 cudaError_t launch_emit_fountain(uint64_t seed, uint32_t step, uint32_t n, const float center[3], float radius,
@@ -170,16 +210,29 @@ cudaError_t launch_splat(const DevBufs &b, uint32_t n, int layout_sorted, uint32
                          float half_v, float scale_u, float scale_v, uint32_t width, uint32_t height,
                          uint32_t *count, float *depth, cudaStream_t st);
 
+// Working memory of a reference-grid build of n particles and C cells: counts and cursors (C
+// words each), slot ids (n), scan block sums (C / kScanTile + 1), crowded cells (big_words(n)).
+struct GridScratch {
+    uint32_t *count, *cursor, *tmp, *bsum, *big;
+};
+// the reference's grid (cells of size h) of n id-ordered float positions (sph_noalloc.cu)
+cudaError_t ref_grid_build(const float *xyz, uint32_t n, int3 res, float3 half, float h, uint32_t *out_cell,
+                           uint32_t *out_start, uint32_t *out_order, const GridScratch &g, cudaStream_t st);
+
 // checked builds: OR each translation unit's device check flags into *out and clear them
 cudaError_t check_flags_kernels(uint32_t *out);
 cudaError_t check_flags_mixed(uint32_t *out);
 cudaError_t check_flags_handoff(uint32_t *out);
+cudaError_t check_flags_noalloc(uint32_t *out);
 
 // mixed-precision passes (sph_mixed.cu)
 cudaError_t mixed_permute(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, cudaStream_t st);
-cudaError_t mixed_density(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, cudaStream_t st);
-cudaError_t mixed_forces(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, bool record_acc,
-                         cudaStream_t st);
+cudaError_t mixed_density(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, int cell_mult,
+                          cudaStream_t st);
+// variant: the mixed force pass's launch form, 0..kMixedVariants-1 (all give the same bits)
+constexpr int kMixedVariants = 4;
+cudaError_t mixed_forces(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, bool record_acc, int variant,
+                         int cell_mult, cudaStream_t st);
 cudaError_t mixed_egress(const DevBufs &b, uint32_t n_state, uint32_t n_aux, uint32_t n_acc, int layout_sorted,
                          int aux_sorted, bool f64, cudaStream_t st);
 

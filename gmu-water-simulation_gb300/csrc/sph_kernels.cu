@@ -123,8 +123,10 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &t
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *__restrict__ count, uint32_t ncells,
-                                                              uint32_t *__restrict__ bsum, bool vec)
+                                                              uint32_t *__restrict__ bsum, bool vec,
+                                                              uint32_t *__restrict__ big)
 {
+    if (big && blockIdx.x == 0 && threadIdx.x == 0) big[0] = 0;  // the apply phase lists this step's big cells
     const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
     const uint4 c4 = load_counts4(count, base, ncells, vec);
     uint32_t s = c4.x + c4.y + c4.z + c4.w;
@@ -144,7 +146,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *__
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t *__restrict__ count, uint32_t ncells,
                                                              const uint32_t *__restrict__ bsum,
                                                              uint32_t *__restrict__ start,
-                                                             uint32_t *__restrict__ cursor, bool vec)
+                                                             uint32_t *__restrict__ cursor, bool vec,
+                                                             uint32_t *__restrict__ big)
 {
     const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
     const uint4 c4 = load_counts4(count, base, ncells, vec);
@@ -163,6 +166,12 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t *__restric
     const uint32_t run = block_exclusive_scan(c4.x + c4.y + c4.z + c4.w, total) + off;
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) start[ncells] = off + total;
     const uint4 st4v = make_uint4(run, run + c4.x, run + c4.x + c4.y, run + c4.x + c4.y + c4.z);
+    if (big) {  // cells above kBigCell particles get their slot ids sorted before the rank
+        const uint32_t cv[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (cv[k] > kBigCell) big[1 + atomicAdd(big, 1u)] = base + (uint32_t) k;
+    }
     if (vec && base + 4 <= ncells) {
         *reinterpret_cast<uint4 *>(start + base) = st4v;
         *reinterpret_cast<uint4 *>(cursor + base) = st4v;
@@ -201,6 +210,42 @@ __global__ void __launch_bounds__(256) k_slot(const uint2 *__restrict__ cid_u, u
     if (sph_check(t < n, CHK_SORT)) tmp[t] = cd.y;
 }
 
+// Slot ids of the listed big cells sorted ascending in place (one block per cell at a time,
+// bitonic sort in shared memory over the cell's ids padded to a power of two). Cells above
+// kBigCellMax are left as they are: rank_in_cell counts them.
+constexpr int SORT_THREADS = 256;
+
+__global__ void __launch_bounds__(SORT_THREADS) k_sort_big(const uint32_t *__restrict__ start, uint32_t *__restrict__ tmp,
+                                                           const uint32_t *__restrict__ big)
+{
+    __shared__ uint32_t sk[kBigCellMax];
+    const uint32_t nbig = big[0];
+    for (uint32_t q = blockIdx.x; q < nbig; q += gridDim.x) {
+        const uint32_t cell = big[1 + q];
+        const uint32_t b = start[cell], e = start[cell + 1], occ = e - b;
+        if (occ <= kBigCell || occ > kBigCellMax) continue;
+        uint32_t P = 2 * kBigCell;
+        while (P < occ) P <<= 1;
+        for (uint32_t t = threadIdx.x; t < P; t += SORT_THREADS) sk[t] = t < occ ? tmp[b + t] : 0xffffffffu;
+        __syncthreads();
+        for (uint32_t k = 2; k <= P; k <<= 1) {
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                for (uint32_t t = threadIdx.x; t < P / 2; t += SORT_THREADS) {
+                    const uint32_t lo = 2 * j * (t / j) + (t % j), hi = lo + j;  // lo has bit j clear
+                    const uint32_t x = sk[lo], y = sk[hi];
+                    if ((x > y) == ((lo & k) == 0)) {
+                        sk[lo] = y;
+                        sk[hi] = x;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (uint32_t t = threadIdx.x; t < occ; t += SORT_THREADS) tmp[b + t] = sk[t];
+        __syncthreads();
+    }
+}
+
 template <class R>
 __global__ void __launch_bounds__(256) k_rank_permute(const uint2 *__restrict__ cid_u, uint32_t n,
                                                       const uint32_t *__restrict__ start,
@@ -214,9 +259,7 @@ __global__ void __launch_bounds__(256) k_rank_permute(const uint2 *__restrict__ 
     const uint2 cd = cid_u[i];
     const uint32_t b = start[cd.x], e = start[cd.x + 1];
     if (!sph_check(b <= e && e <= n, CHK_SORT)) return;
-    uint32_t r = 0;
-    for (uint32_t k = b; k < e; k++) r += tmp[k] < cd.y ? 1u : 0u;
-    const uint32_t dst = b + r;
+    const uint32_t dst = b + rank_in_cell(tmp, b, e, cd.y);
     if (!sph_check(dst < e, CHK_SORT)) return;
     st4(pos_s + dst, ld4(pos_u + i));
     st4(vel_s + dst, ld4(vel_u + i));
@@ -358,20 +401,21 @@ __global__ void __launch_bounds__(BLOCK) k_forces_list(
 
 // ------------------------------------------------------------------------------------
 // Neighbour masks: the density pass already tests every candidate, so it records which ones
-// it accepted. For each particle and each of its 9 rows, the row's candidate window
-// [start of cell x-1, end of cell x+1) is cut into 32-candidate chunks; chunk w of row r is
-// one 32-bit word at masks[(r * MASK_WORDS + w) * n + i] (coalesced across particles). Bit k
+// it accepted. For each particle and each row of its stencil, the row's candidate window
+// [start of cell x-RAD, end of cell x+RAD) is cut into 32-candidate chunks; chunk w of row r is
+// one 32-bit word at masks[(r * WORDS + w) * n + i] (coalesced across particles). Bit k
 // set = candidate window_start + 32 w + k is a neighbour (self included). Candidates past
-// MASK_WORDS chunks are not recorded: the force pass tests them itself.
+// WORDS chunks are not recorded: the force pass tests them itself. RAD = 1 is the reference's
+// 27 cells of size h; RAD = 2 walks 125 cells of size h/2 (42% less volume than 27 h^3).
 
-template <class R, bool REC>
-__global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
-                                                      const uint32_t *__restrict__ start,
-                                                      const SceneDev *__restrict__ scenes, uint32_t n, Consts<R> c,
-                                                      uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ vel,
-                                                      Vec4<R> *__restrict__ frec)
+template <class R, bool REC, int RAD>
+__device__ __forceinline__ void density_mask_one(uint32_t i, const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
+                                                 const uint32_t *__restrict__ start,
+                                                 const SceneDev *__restrict__ scenes, uint32_t n, const Consts<R> &c,
+                                                 uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ vel,
+                                                 Vec4<R> *__restrict__ frec)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    using St = Stencil<RAD>;
     if (i >= n) return;
     const Vec4<R> pi = ld4(pos + i);
     const SceneDev sc = load_scene(scenes, wbits(pi.w));
@@ -379,34 +423,26 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
     hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
     const R h2 = c.h2;
     R acc = 0;
-    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
-    const int xl = cx > 0 ? cx - 1 : 0, xh = cx + 1 < X ? cx + 1 : X - 1;
 #pragma unroll 1
-    for (int dz = -1; dz <= 1; dz++) {
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; dy++) {
-            const int r = (dz + 1) * 3 + (dy + 1);
-            const int z = cz + dz, y = cy + dy;
-            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
-            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
-            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
-            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
-            int w = 0;
-            for (uint32_t cb = jb; cb < je; cb += 32, w++) {
-                // bit k of the chunk's word = candidate cb + k; bits enter at the top and
-                // move down one place per candidate
-                const uint32_t ce = min(je, cb + 32u);
-                uint32_t m = 0;
+    for (int r = 0; r < St::ROWS; r++) {
+        uint32_t jb, je;
+        if (!stencil_row<RAD>(sc, start, cx, cy, cz, r, jb, je)) continue;
+        if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
+        int w = 0;
+        for (uint32_t cb = jb; cb < je; cb += 32, w++) {
+            // bit k of the chunk's word = candidate cb + k; bits enter at the top and
+            // move down one place per candidate
+            const uint32_t ce = min(je, cb + 32u);
+            uint32_t m = 0;
 #pragma unroll 4
-                for (uint32_t j = cb; j < ce; j++) {
-                    const Vec4<R> pj = ld4(pos + j);
-                    const R t = h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
-                    m = (m >> 1) | (t > (R) 0 ? 0x80000000u : 0u);
-                    acc = poly6_acc<R>(acc, t);
-                }
-                m >>= 32 - (ce - cb);
-                if (w < MASK_WORDS) masks[(size_t) (r * MASK_WORDS + w) * n + i] = m;
+            for (uint32_t j = cb; j < ce; j++) {
+                const Vec4<R> pj = ld4(pos + j);
+                const R t = h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
+                m = (m >> 1) | (t > (R) 0 ? 0x80000000u : 0u);
+                acc = poly6_acc<R>(acc, t);
             }
+            m >>= 32 - (ce - cb);
+            if (w < St::WORDS) masks[(size_t) (r * St::WORDS + w) * n + i] = m;
         }
     }
     const R rho = rmul(rmul(acc, c.c_poly6), c.mass);
@@ -419,6 +455,45 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
         st4(frec + 2 * (size_t) i, Vec4<R>{pi.x, pi.y, pi.z, q});
         st4(frec + 2 * (size_t) i + 1, Vec4<R>{vi.x, vi.y, vi.z, inv});
     }
+}
+
+template <class R, bool REC, int RAD = 1>
+__global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
+                                                      const uint32_t *__restrict__ start,
+                                                      const SceneDev *__restrict__ scenes, uint32_t n, Consts<R> c,
+                                                      uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ vel,
+                                                      Vec4<R> *__restrict__ frec)
+{
+    density_mask_one<R, REC, RAD>(blockIdx.x * blockDim.x + threadIdx.x, pos, aux, start, scenes, n, c, masks, vel,
+                                  frec);
+}
+
+// Persistent forms of the neighbour passes: as many resident blocks as fit on the GPU, each
+// taking the next tile of BLOCK consecutive particles from a counter until none is left, so that
+// SMs that finish their tiles early (sparse regions, small scenes of a batch) take more. The
+// counter (tiles[0]) is zeroed before each launch. Same per-particle work and bits as the flat
+// launches.
+__device__ __forceinline__ bool next_tile(uint32_t *__restrict__ tiles, uint32_t &tile)
+{
+    __shared__ uint32_t t;
+    if (threadIdx.x == 0) t = atomicAdd(tiles, 1u);
+    __syncthreads();
+    tile = t;
+    __syncthreads();
+    return true;
+}
+
+template <class R, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_density_mask_persist(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
+                                                                const uint32_t *__restrict__ start,
+                                                                const SceneDev *__restrict__ scenes, uint32_t n,
+                                                                Consts<R> c, uint32_t *__restrict__ masks,
+                                                                const Vec4<R> *__restrict__ vel,
+                                                                Vec4<R> *__restrict__ frec, uint32_t *__restrict__ tiles)
+{
+    uint32_t tile;
+    while (next_tile(tiles, tile) && (uint64_t) tile * BLOCK < n)
+        density_mask_one<R, true, 1>(tile * BLOCK + threadIdx.x, pos, aux, start, scenes, n, c, masks, vel, frec);
 }
 
 // Forces driven by the density pass's masks: only accepted neighbours are visited, in the
@@ -457,8 +532,8 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask(
             for (uint32_t w = 0; w < nw; w++) {
                 const uint32_t cb = jb + 32 * w;
                 uint32_t m = 0;
-                if (w < (uint32_t) MASK_WORDS) {
-                    m = __ldg(masks + (size_t) (r * MASK_WORDS + w) * n + i);
+                if (w < (uint32_t) Stencil<1>::WORDS) {
+                    m = __ldg(masks + (size_t) (r * Stencil<1>::WORDS + w) * n + i);
                 } else {  // beyond the recorded chunks: test the candidates here
                     const uint32_t ce = min(je, cb + 32u);
                     for (uint32_t j = ce; j-- > cb;) {
@@ -487,16 +562,16 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask(
 // Forces from the masks, two accepted neighbours per iteration: both neighbours' records are
 // loaded before either's terms are added, so two gathers are in flight at once and the loop
 // overhead is paid once per pair. The terms are still added one neighbour at a time in
-// candidate order (the sums are the same bits as the other forms).
-template <class R, int MINB, bool REC, int BLOCK = 256>
-__global__ void __launch_bounds__(BLOCK, MINB) k_forces_mask2(
-    const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
+// candidate order (the sums are the same bits as the other forms of the same cell multiple).
+template <class R, bool REC, int RAD>
+__device__ __forceinline__ void forces_mask2_one(
+    uint32_t i, const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
     const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
-    uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ frec,
+    uint32_t n, const Consts<R> &c, const uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ frec,
     Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out,
     uint2 *__restrict__ cid_out, uint32_t *__restrict__ count)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    using St = Stencil<RAD>;
     if (i >= n) return;
     const Vec4<R> pi = ld4(pos + i);
     const Vec4<R> vi = ld4(vel + i);
@@ -506,60 +581,55 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_forces_mask2(
     hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
     const R h2 = c.h2, qi = ai.z;
     R fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
-    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
-    const int xl = cx > 0 ? cx - 1 : 0, xh = cx + 1 < X ? cx + 1 : X - 1;
 #pragma unroll 1
-    for (int dz = -1; dz <= 1; dz++) {
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; dy++) {
-            const int r = (dz + 1) * 3 + (dy + 1);
-            const int z = cz + dz, y = cy + dy;
-            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
-            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
-            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
-            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
-            const uint32_t nw = (je - jb + 31) / 32;
-            // the row's recorded words loaded together at the start of the row
-            const uint32_t *mr = masks + (size_t) (r * MASK_WORDS) * n + i;
-            const uint32_t w0 = nw > 0 ? __ldg(mr) : 0u, w1 = nw > 1 ? __ldg(mr + n) : 0u;
-            const uint32_t w2 = nw > 2 ? __ldg(mr + 2 * (size_t) n) : 0u, w3 = nw > 3 ? __ldg(mr + 3 * (size_t) n) : 0u;
-            for (uint32_t w = 0; w < nw; w++) {
-                const uint32_t cb = jb + 32 * w;
-                uint32_t m = 0;
-                if (w < (uint32_t) MASK_WORDS) {
-                    m = w == 0 ? w0 : w == 1 ? w1 : w == 2 ? w2 : w3;
-                } else {  // beyond the recorded chunks: test the candidates here
-                    const uint32_t ce = min(je, cb + 32u);
-                    for (uint32_t j = ce; j-- > cb;) {
-                        const Vec4<R> pj = ld4(pos + j);
-                        m = (m << 1) | (h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2) > (R) 0 ? 1u : 0u);
-                    }
+    for (int r = 0; r < St::ROWS; r++) {
+        uint32_t jb, je;
+        if (!stencil_row<RAD>(sc, start, cx, cy, cz, r, jb, je)) continue;
+        if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
+        const uint32_t nw = (je - jb + 31) / 32;
+        // the row's recorded words loaded together at the start of the row
+        const uint32_t *mr = masks + (size_t) (r * St::WORDS) * n + i;
+        uint32_t wr[St::WORDS];
+#pragma unroll
+        for (int k = 0; k < St::WORDS; k++) wr[k] = nw > (uint32_t) k ? __ldg(mr + k * (size_t) n) : 0u;
+        for (uint32_t w = 0; w < nw; w++) {
+            const uint32_t cb = jb + 32 * w;
+            uint32_t m = 0;
+            if (w < (uint32_t) St::WORDS) {
+                m = wr[0];
+#pragma unroll
+                for (int k = 1; k < St::WORDS; k++) m = w == (uint32_t) k ? wr[k] : m;
+            } else {  // beyond the recorded chunks: test the candidates here
+                const uint32_t ce = min(je, cb + 32u);
+                for (uint32_t j = ce; j-- > cb;) {
+                    const Vec4<R> pj = ld4(pos + j);
+                    m = (m << 1) | (h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2) > (R) 0 ? 1u : 0u);
                 }
-                if (i - cb < 32u) m &= ~(1u << (i - cb));  // the particle itself
-                while (m) {
-                    const uint32_t j0 = cb + (uint32_t) (__ffs(m) - 1);
-                    m &= m - 1;
-                    const bool two = m != 0;
-                    const uint32_t j1 = two ? cb + (uint32_t) (__ffs(m) - 1) : j0;
-                    m &= m - 1;
-                    if (!sph_check(j0 < je && j1 < je, CHK_NEIGHBOUR)) continue;
-                    Vec4<R> p0, v0, p1, v1;
-                    R q0, inv0, q1, inv1;
-                    if (REC) {
-                        p0 = ld4(frec + 2 * (size_t) j0);
-                        v0 = ld4(frec + 2 * (size_t) j0 + 1);
-                        p1 = ld4(frec + 2 * (size_t) j1);
-                        v1 = ld4(frec + 2 * (size_t) j1 + 1);
-                        q0 = p0.w, inv0 = v0.w, q1 = p1.w, inv1 = v1.w;
-                    } else {
-                        p0 = ld4(pos + j0), v0 = ld4(vel + j0);
-                        p1 = ld4(pos + j1), v1 = ld4(vel + j1);
-                        ld_qinv(aux + j0, q0, inv0);
-                        ld_qinv(aux + j1, q1, inv1);
-                    }
-                    pair_terms<R>(pi, vi, qi, p0, v0, q0, inv0, c, fpx, fpy, fpz, fvx, fvy, fvz);
-                    if (two) pair_terms<R>(pi, vi, qi, p1, v1, q1, inv1, c, fpx, fpy, fpz, fvx, fvy, fvz);
+            }
+            if (i - cb < 32u) m &= ~(1u << (i - cb));  // the particle itself
+            while (m) {
+                const uint32_t j0 = cb + (uint32_t) (__ffs(m) - 1);
+                m &= m - 1;
+                const bool two = m != 0;
+                const uint32_t j1 = two ? cb + (uint32_t) (__ffs(m) - 1) : j0;
+                m &= m - 1;
+                if (!sph_check(j0 < je && j1 < je, CHK_NEIGHBOUR)) continue;
+                Vec4<R> p0, v0, p1, v1;
+                R q0, inv0, q1, inv1;
+                if (REC) {
+                    p0 = ld4(frec + 2 * (size_t) j0);
+                    v0 = ld4(frec + 2 * (size_t) j0 + 1);
+                    p1 = ld4(frec + 2 * (size_t) j1);
+                    v1 = ld4(frec + 2 * (size_t) j1 + 1);
+                    q0 = p0.w, inv0 = v0.w, q1 = p1.w, inv1 = v1.w;
+                } else {
+                    p0 = ld4(pos + j0), v0 = ld4(vel + j0);
+                    p1 = ld4(pos + j1), v1 = ld4(vel + j1);
+                    ld_qinv(aux + j0, q0, inv0);
+                    ld_qinv(aux + j1, q1, inv1);
                 }
+                pair_terms<R>(pi, vi, qi, p0, v0, q0, inv0, c, fpx, fpy, fpz, fvx, fvy, fvz);
+                if (two) pair_terms<R>(pi, vi, qi, p1, v1, q1, inv1, c, fpx, fpy, fpz, fvx, fvy, fvz);
             }
         }
     }
@@ -567,6 +637,32 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_forces_mask2(
     const SceneDev sc2 = load_scene(scenes, wbits(pi.w));
     finish_particle<R>(i, pi, vi, ai.x, sc2, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
                        cid_out, count);
+}
+
+template <class R, int MINB, bool REC, int BLOCK = 256, int RAD = 1>
+__global__ void __launch_bounds__(BLOCK, MINB) k_forces_mask2(
+    const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
+    const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
+    uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ frec,
+    Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out,
+    uint2 *__restrict__ cid_out, uint32_t *__restrict__ count)
+{
+    forces_mask2_one<R, REC, RAD>(blockIdx.x * BLOCK + threadIdx.x, pos, vel, aux, start, scenes, obstacles, n, c,
+                                  masks, frec, pos_out, vel_out, acc_out, cid_out, count);
+}
+
+template <class R, int MINB, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, MINB) k_forces_mask2_persist(
+    const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
+    const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
+    uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ frec,
+    Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out,
+    uint2 *__restrict__ cid_out, uint32_t *__restrict__ count, uint32_t *__restrict__ tiles)
+{
+    uint32_t tile;
+    while (next_tile(tiles, tile) && (uint64_t) tile * BLOCK < n)
+        forces_mask2_one<R, true, 1>(tile * BLOCK + threadIdx.x, pos, vel, aux, start, scenes, obstacles, n, c, masks,
+                                     frec, pos_out, vel_out, acc_out, cid_out, count);
 }
 
 // All-pairs forms, the reference's brute-force simulator (sph_brute.cl:9-57) restated: every
@@ -733,6 +829,24 @@ __global__ void __launch_bounds__(256) k_density_blk(const Vec4<R> *__restrict__
 }
 
 // ------------------------------------------------------------------------------------
+// rehash: the (cell, id) of every *_u particle again, its cell in the step grid (after the grid's
+// cell multiple changed, or after the *_u arrays were refilled); the counts must have been zeroed.
+template <class R>
+__global__ void __launch_bounds__(256) k_rehash(const Vec4<R> *__restrict__ pos_u, const Vec4<R> *__restrict__ vel_u,
+                                                uint2 *__restrict__ cid_u, uint32_t *__restrict__ count,
+                                                const SceneDev *__restrict__ scenes, uint32_t n, Consts<R> c)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Vec4<R> p = ldc4(pos_u + i);
+    const SceneDev sc = load_scene(scenes, wbits(p.w));
+    int cx, cy, cz;
+    const uint32_t cell = hash_cell<R>(sc, p.x, p.y, p.z, c, cx, cy, cz);
+    atomicAdd(count + cell, 1u);
+    cid_u[i] = make_uint2(cell, wbits(ldc4(vel_u + i).w));
+}
+
+// ------------------------------------------------------------------------------------
 // egress: any layout -> id-ordered, scene-major staging arrays for one D2H copy each.
 template <class R>
 __global__ void __launch_bounds__(256) k_egress(const Vec4<R> *__restrict__ posL, const Vec4<R> *__restrict__ velL,
@@ -834,6 +948,19 @@ __global__ void k_stats_final(const double *__restrict__ partial, const uint32_t
 // ------------------------------------------------------------------------------------
 static inline unsigned nblk(uint32_t n, unsigned t) { return (unsigned) ((n + t - 1) / t); }
 
+// Grid of a persistent launch: as many blocks as are resident at once on the current device.
+template <class K>
+static unsigned resident_grid(K kernel, int block)
+{
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, 0) != cudaSuccess || per < 1 || sms < 1) {
+        cudaGetLastError();
+        return 1024;  // any grid is correct: the tiles are fetched until none is left
+    }
+    return (unsigned) (sms * per);
+}
+
 template <class R>
 cudaError_t Launch<R>::ingest(const DevBufs &b, const float *xyz, const float *vel, uint32_t first, uint32_t n,
                               int32_t scene, uint32_t id0, uint32_t nscenes, Consts<R> c, cudaStream_t st)
@@ -851,8 +978,8 @@ cudaError_t Launch<R>::scan(const DevBufs &b, uint32_t ncells, cudaStream_t st)
     // 16-byte accesses only where all three arrays allow them (a caller's start array may not)
     const bool vec = ((reinterpret_cast<uintptr_t>(b.count) | reinterpret_cast<uintptr_t>(b.start) |
                        reinterpret_cast<uintptr_t>(b.cursor)) & 15u) == 0;
-    k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, vec);
-    k_scan_apply<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, b.start, b.cursor, vec);
+    k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, vec, b.big);
+    k_scan_apply<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, b.start, b.cursor, vec, b.big);
     return cudaGetLastError();
 }
 
@@ -861,9 +988,20 @@ cudaError_t Launch<R>::permute(const DevBufs &b, uint32_t n, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
     k_slot<<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.cursor, b.tmp);
+    cudaError_t e = launch_sort_big(b.start, b.tmp, b.big, st);
+    if (e != cudaSuccess) return e;
     k_rank_permute<R><<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.start, b.tmp, (const Vec4<R> *) b.pos_u,
                                                     (const Vec4<R> *) b.vel_u, (Vec4<R> *) b.pos_s,
                                                     (Vec4<R> *) b.vel_s);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t Launch<R>::rehash(const DevBufs &b, uint32_t n, Consts<R> c, cudaStream_t st)
+{
+    if (!n) return cudaSuccess;
+    k_rehash<R><<<nblk(n, 256), 256, 0, st>>>((const Vec4<R> *) b.pos_u, (const Vec4<R> *) b.vel_u, b.cid_u, b.count,
+                                              b.scenes, n, c);
     return cudaGetLastError();
 }
 
@@ -877,11 +1015,28 @@ cudaError_t Launch<R>::density(const DevBufs &b, uint32_t n, Consts<R> c, const 
         k_density_all<R><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c);
         return cudaGetLastError();
     }
-    if (t.forces_mode >= 7) {  // masks and force records
-        k_density_mask<R, true><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c, b.masks,
-                                                              (const Vec4<R> *) b.vel_s, (Vec4<R> *) b.frec);
+    if (t.forces_mode == 12) {  // persistent launch over tiles of 256 particles
+        if (t.cell_mult != 1) return cudaErrorInvalidValue;
+        cudaError_t e = cudaMemsetAsync(b.tiles, 0, 4, st);
+        if (e != cudaSuccess) return e;
+        k_density_mask_persist<R, 256><<<resident_grid(k_density_mask_persist<R, 256>, 256), 256, 0, st>>>(
+            pos, aux, b.start, b.scenes, n, c, b.masks, (const Vec4<R> *) b.vel_s, (Vec4<R> *) b.frec, b.tiles);
         return cudaGetLastError();
     }
+    if (t.forces_mode >= 7) {  // masks and force records
+        if (t.cell_mult == 2) {
+            if constexpr (sizeof(R) == 4)
+                k_density_mask<R, true, 2><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c, b.masks,
+                                                                         (const Vec4<R> *) b.vel_s, (Vec4<R> *) b.frec);
+            else
+                return cudaErrorInvalidValue;  // the FP64 form runs on the reference's grid only
+        } else {
+            k_density_mask<R, true><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c, b.masks,
+                                                                  (const Vec4<R> *) b.vel_s, (Vec4<R> *) b.frec);
+        }
+        return cudaGetLastError();
+    }
+    if (t.cell_mult != 1) return cudaErrorInvalidValue;  // cells of h/2: the record variants only
     if (t.forces_mode >= 3) {  // the mask-driven force passes need the masks
         k_density_mask<R, false><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c, b.masks, nullptr,
                                                                nullptr);
@@ -896,6 +1051,15 @@ cudaError_t Launch<R>::density(const DevBufs &b, uint32_t n, Consts<R> c, const 
     return cudaGetLastError();
 }
 
+// the record-reading force kernel of one (register budget, block size, stencil) choice
+template <class R, int MINB, int BLOCK, int RAD>
+static void launch_forces_rec(const DevBufs &b, uint32_t n, Consts<R> c, Vec4<R> *ao, cudaStream_t st)
+{
+    k_forces_mask2<R, MINB, true, BLOCK, RAD><<<nblk(n, BLOCK), BLOCK, 0, st>>>(
+        (const Vec4<R> *) b.pos_s, (const Vec4<R> *) b.vel_s, (const Vec4<R> *) b.aux, b.start, b.scenes, b.obstacles,
+        n, c, b.masks, (const Vec4<R> *) b.frec, (Vec4<R> *) b.pos_u, (Vec4<R> *) b.vel_u, ao, b.cid_u, b.count);
+}
+
 template <class R>
 cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool record_acc, const Tune &t,
                               cudaStream_t st)
@@ -903,6 +1067,21 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
     if (!n) return cudaSuccess;
     const Vec4<R> *pos = (const Vec4<R> *) b.pos_s, *vel = (const Vec4<R> *) b.vel_s, *aux = (const Vec4<R> *) b.aux;
     Vec4<R> *po = (Vec4<R> *) b.pos_u, *vo = (Vec4<R> *) b.vel_u, *ao = record_acc ? (Vec4<R> *) b.acc : nullptr;
+    if (t.cell_mult == 2) {  // cells of h/2: the record variants 7 to 11 (plain FP32 only)
+        if constexpr (sizeof(R) == 4) {
+            switch (t.forces_mode) {
+            case 7: launch_forces_rec<R, 1, 256, 2>(b, n, c, ao, st); break;
+            case 8: launch_forces_rec<R, 5, 256, 2>(b, n, c, ao, st); break;
+            case 9: launch_forces_rec<R, 6, 256, 2>(b, n, c, ao, st); break;
+            case 10: launch_forces_rec<R, 12, 128, 2>(b, n, c, ao, st); break;
+            case 11: launch_forces_rec<R, 10, 128, 2>(b, n, c, ao, st); break;
+            default: return cudaErrorInvalidValue;
+            }
+            return cudaGetLastError();
+        } else {
+            return cudaErrorInvalidValue;
+        }
+    }
     switch (t.forces_mode) {
     case Tune::ALL_PAIRS:
         k_forces_all<R><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c, po, vo, ao,
@@ -949,6 +1128,14 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
                                                                        n, c, b.masks, (const Vec4<R> *) b.frec, po, vo,
                                                                        ao, b.cid_u, b.count);
         break;
+    case 12: {  // variant 10's kernel as a persistent launch over tiles of 128 particles
+        cudaError_t e = cudaMemsetAsync(b.tiles + 1, 0, 4, st);
+        if (e != cudaSuccess) return e;
+        k_forces_mask2_persist<R, 12, 128><<<resident_grid(k_forces_mask2_persist<R, 12, 128>, 128), 128, 0, st>>>(
+            pos, vel, aux, b.start, b.scenes, b.obstacles, n, c, b.masks, (const Vec4<R> *) b.frec, po, vo, ao, b.cid_u,
+            b.count, b.tiles + 1);
+        break;
+    }
     case 1:
         k_forces_list<R, 32, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
                                                                   po, vo, ao, b.cid_u, b.count);
@@ -1001,6 +1188,15 @@ cudaError_t launch_slot(const DevBufs &b, uint32_t n, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
     k_slot<<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.cursor, b.tmp);
+    return launch_sort_big(b.start, b.tmp, b.big, st);
+}
+
+cudaError_t launch_sort_big(const uint32_t *start, uint32_t *tmp, const uint32_t *big, cudaStream_t st)
+{
+    if (!big) return cudaSuccess;
+    // a fixed grid walks the list (its length is known only on the device); with no big cell
+    // every block returns at once
+    k_sort_big<<<152, SORT_THREADS, 0, st>>>(start, tmp, big);
     return cudaGetLastError();
 }
 

@@ -9,7 +9,10 @@
 //    it wraps to a magnitude above h, so the neighbour test still rejects the pair (every
 //    neighbour candidate is within 7 h unless a particle has been pushed more than ~5 h
 //    outside the box);
-//  - neighbour velocities are gathered in FP16 (8 bytes instead of 16);
+//  - the force pass reads each neighbour from one packed 16-byte record that the density pass
+//    writes: the three 16-bit position codes, the FP16 velocity, and the neighbour's two force
+//    factors p/rho^2 and 1/rho in FP16, scaled by 2^10 and 2^14 into FP16's normal range
+//    (relative rounding error at most 2^-11 each; the particle's own factors stay FP32);
 //  - density sums are compensated FP32 sums: each 32-candidate chunk is summed, and the chunk
 //    sums are added with Kahan compensation;
 //  - each particle's position is a hi/lo FP32 pair through the integration (TwoSum), and the
@@ -47,20 +50,30 @@ __device__ __forceinline__ void code_delta(uint2 gi, uint2 gj, float &dx, float 
     dz = (float) (int16_t) ((gi.y - gj.y) & 0xffffu);
 }
 
-__device__ __forceinline__ uint2 pack_half3(float x, float y, float z)
+__device__ __forceinline__ uint32_t pack_half2(float lo, float hi)
 {
-    const __half2 a = __floats2half2_rn(x, y);
-    const __half2 b = __floats2half2_rn(z, 0.0f);
-    return make_uint2(*reinterpret_cast<const uint32_t *>(&a), *reinterpret_cast<const uint32_t *>(&b));
+    const __half2 a = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&a);
 }
 
-__device__ __forceinline__ void unpack_half3(uint2 v, float &x, float &y, float &z)
+__device__ __forceinline__ float2 unpack_half2(uint32_t v)
 {
-    const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&v.x));
-    const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&v.y));
-    x = a.x;
-    y = a.y;
-    z = b.x;
+    return __half22float2(*reinterpret_cast<const __half2 *>(&v));
+}
+
+// Scales of the FP16 force factors in the neighbour record: p/rho^2 lies in [-0.03, 0.001] and
+// 1/rho in (0, 1/328] (a density always includes the particle's own term, m poly6(0) = 328.3), so
+// these bring both into FP16's normal range with room on either side.
+constexpr float Q_SCALE = 1024.0f;       // p / rho^2 * 2^10
+constexpr float INV_SCALE = 16384.0f;    // 1 / rho * 2^14
+
+// The force pass's view of a neighbour, one 16-byte record:
+//   x: codes x | y << 16; y: code z | FP16 vx << 16; z: FP16 vy | FP16 vz << 16;
+//   w: FP16 (p/rho^2 * 2^10) | FP16 (1/rho * 2^14) << 16
+__device__ __forceinline__ uint4 make_record(uint2 g, float vx, float vy, float vz, float q, float inv)
+{
+    return make_uint4(g.x, (g.y & 0xffffu) | (pack_half2(vx, 0.0f) << 16), pack_half2(vy, vz),
+                      pack_half2(q * Q_SCALE, inv * INV_SCALE));
 }
 
 // ---- grid: canonical rank + permute, writing the master state and the gather records ----
@@ -68,16 +81,14 @@ __global__ void __launch_bounds__(256) k_rank_permute_mixed(
     const uint2 *__restrict__ cid_u, uint32_t n, const uint32_t *__restrict__ start, const uint32_t *__restrict__ tmp,
     const Vec4<float> *__restrict__ pos_u, const Vec4<float> *__restrict__ lo_u, const Vec4<float> *__restrict__ vel_u,
     const SceneDev *__restrict__ scenes, Consts<float> c, MixConsts mc, Vec4<float> *__restrict__ pos_s,
-    Vec4<float> *__restrict__ lo_s, Vec4<float> *__restrict__ vel_s, uint2 *__restrict__ gpos, uint2 *__restrict__ gvel)
+    Vec4<float> *__restrict__ lo_s, Vec4<float> *__restrict__ vel_s, uint2 *__restrict__ gpos)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 cd = cid_u[i];
     const uint32_t b = start[cd.x], e = start[cd.x + 1];
     if (!sph_check(b <= e && e <= n, CHK_SORT)) return;
-    uint32_t r = 0;
-    for (uint32_t k = b; k < e; k++) r += tmp[k] < cd.y ? 1u : 0u;
-    const uint32_t dst = b + r;
+    const uint32_t dst = b + rank_in_cell(tmp, b, e, cd.y);
     if (!sph_check(dst < e, CHK_SORT)) return;
     const Vec4<float> p = ld4(pos_u + i), lo = ld4(lo_u + i), v = ld4(vel_u + i);
     st4(pos_s + dst, p);
@@ -88,7 +99,6 @@ __global__ void __launch_bounds__(256) k_rank_permute_mixed(
     const uint32_t qy = axis_code(p.y, lo.y, sc.half[1], c.h, c.inv_h_f, mc.to_units);
     const uint32_t qz = axis_code(p.z, lo.z, sc.half[2], c.h, c.inv_h_f, mc.to_units);
     gpos[dst] = make_uint2(qx | (qy << 16), qz);
-    gvel[dst] = pack_half3(v.x, v.y, v.z);
 }
 
 // Kahan step with explicitly rounded operations (no reassociation, no fused multiply-add)
@@ -101,12 +111,15 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float term)
 }
 
 // ---- density: neighbour masks (as the plain mask kernel), compensated sums ---------------
+template <int RAD>
 __global__ void __launch_bounds__(128) k_density_mixed(const Vec4<float> *__restrict__ pos,
                                                        const uint2 *__restrict__ gpos, Vec4<float> *__restrict__ aux,
                                                        const uint32_t *__restrict__ start,
                                                        const SceneDev *__restrict__ scenes, uint32_t n,
-                                                       Consts<float> c, MixConsts mc, uint32_t *__restrict__ masks)
+                                                       Consts<float> c, MixConsts mc, uint32_t *__restrict__ masks,
+                                                       const Vec4<float> *__restrict__ vel, uint4 *__restrict__ rec)
 {
+    using St = Stencil<RAD>;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const Vec4<float> pi = ld4(pos + i);
@@ -115,53 +128,77 @@ __global__ void __launch_bounds__(128) k_density_mixed(const Vec4<float> *__rest
     int cx, cy, cz;
     hash_cell<float>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
     float sum = 0.0f, comp = 0.0f;
-    int r = 0;
-    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
-    const int xl = cx > 0 ? cx - 1 : 0, xh = cx + 1 < X ? cx + 1 : X - 1;
 #pragma unroll 1
-    for (int dz = -1; dz <= 1; dz++) {
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; dy++, r++) {
-            const int z = cz + dz, y = cy + dy;
-            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
-            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
-            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
-            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
-            int w = 0;
-            for (uint32_t cb = jb; cb < je; cb += 32, w++) {
-                // bit k of the chunk's word = candidate cb + k (bits enter at the top)
-                const uint32_t ce = min(je, cb + 32u);
-                uint32_t m = 0;
-                float csum = 0.0f;  // the chunk's terms (at most 32), then one compensated add
+    for (int r = 0; r < St::ROWS; r++) {
+        uint32_t jb, je;
+        if (!stencil_row<RAD>(sc, start, cx, cy, cz, r, jb, je)) continue;
+        if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
+        int w = 0;
+        for (uint32_t cb = jb; cb < je; cb += 32, w++) {
+            // bit k of the chunk's word = candidate cb + k (bits enter at the top)
+            const uint32_t ce = min(je, cb + 32u);
+            uint32_t m = 0;
+            float csum = 0.0f;  // the chunk's terms (at most 32), then one compensated add
 #pragma unroll 4
-                for (uint32_t j = cb; j < ce; j++) {
-                    float x, yy, zz;
-                    code_delta(gi, __ldg(gpos + j), x, yy, zz);
-                    const float t = h2_minus_r2<float>(x, yy, zz, QH2);
-                    m = (m >> 1) | (t > 0.0f ? 0x80000000u : 0u);
-                    csum = poly6_acc<float>(csum, t);
-                }
-                kahan_add(sum, comp, csum);
-                m >>= 32 - (ce - cb);
-                if (w < MASK_WORDS) masks[(size_t) (r * MASK_WORDS + w) * n + i] = m;
+            for (uint32_t j = cb; j < ce; j++) {
+                float x, yy, zz;
+                code_delta(gi, __ldg(gpos + j), x, yy, zz);
+                const float t = h2_minus_r2<float>(x, yy, zz, QH2);
+                m = (m >> 1) | (t > 0.0f ? 0x80000000u : 0u);
+                csum = poly6_acc<float>(csum, t);
             }
+            kahan_add(sum, comp, csum);
+            m >>= 32 - (ce - cb);
+            if (w < St::WORDS) masks[(size_t) (r * St::WORDS + w) * n + i] = m;
         }
     }
     const float rho = __fmul_rn(__fmul_rn(sum, mc.poly6_q), c.mass);
     const float p = __fmul_rn(c.k, __fsub_rn(rho, c.rho0));
-    st4(aux + i, Vec4<float>{rho, p, __fdiv_rn(p, __fmul_rn(rho, rho)), __fdiv_rn(1.0f, rho)});
+    const float q = __fdiv_rn(p, __fmul_rn(rho, rho)), inv = __fdiv_rn(1.0f, rho);
+    st4(aux + i, Vec4<float>{rho, p, q, inv});
+    const Vec4<float> vi = ld4(vel + i);
+    rec[i] = make_record(gi, vi.x, vi.y, vi.z, q, inv);
 }
 
-// ---- forces: mask-driven, code-unit displacements, FP16 neighbour velocities, hi/lo update ----
-__global__ void __launch_bounds__(128, 8) k_forces_mixed(
+// ---- forces: mask-driven, code-unit displacements, one 16-byte record per neighbour ----------
+// Pressure and viscosity terms of one neighbour from its record (the plain form's pair terms in
+// code units; src/CCPUParticleSimulator.cpp:177-183). qs = own p/rho^2 * 2^10.
+__device__ __forceinline__ void mixed_pair(uint2 gi, const Vec4<float> &vi, float qs, uint4 r, const MixConsts &mc,
+                                           float &fpx, float &fpy, float &fpz, float &fvx, float &fvy, float &fvz)
+{
+    float dx, dy, dz;
+    code_delta(gi, make_uint2(r.x, r.y), dx, dy, dz);
+    const float vjx = unpack_half2(r.y >> 16).x;
+    const float2 vyz = unpack_half2(r.z);
+    const float2 qv = unpack_half2(r.w);
+    // at least one unit apart: two particles sharing a code (closer than the 5.6 um resolution)
+    // get no pressure direction rather than a 0/0
+    const float r2 = fmaxf(dx * dx + dy * dy + dz * dz, 1.0f);
+    const float rinv = rsqrtf(r2);
+    const float hr = QUNITS - r2 * rinv;
+    const float wgt = (qs + qv.x) * (mc.spiky_q * (1.0f / Q_SCALE) * hr * hr * rinv);
+    fpx += wgt * dx;
+    fpy += wgt * dy;
+    fpz += wgt * dz;
+    const float l = mc.visc_q * (1.0f / INV_SCALE) * hr * qv.y;
+    fvx += (vjx - vi.x) * l;
+    fvy += (vyz.x - vi.y) * l;
+    fvz += (vyz.y - vi.z) * l;
+}
+
+// Two accepted neighbours per iteration: both records are loaded before either's terms are
+// added (two gathers in flight), the terms still added in candidate order. MINB and BLOCK set
+// the register budget and block size (the launch variants of the mixed form).
+template <int MINB, int BLOCK, int RAD>
+__global__ void __launch_bounds__(BLOCK, MINB) k_forces_mixed(
     const Vec4<float> *__restrict__ pos, const Vec4<float> *__restrict__ lo_s, const Vec4<float> *__restrict__ vel,
-    const Vec4<float> *__restrict__ aux, const uint2 *__restrict__ gpos, const uint2 *__restrict__ gvel,
+    const Vec4<float> *__restrict__ aux, const uint2 *__restrict__ gpos, const uint4 *__restrict__ rec,
     const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
     uint32_t n, Consts<float> c, MixConsts mc, const uint32_t *__restrict__ masks, Vec4<float> *__restrict__ pos_out,
     Vec4<float> *__restrict__ lo_out, Vec4<float> *__restrict__ vel_out, Vec4<float> *__restrict__ acc_out,
     uint2 *__restrict__ cid_out, uint32_t *__restrict__ count)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = blockIdx.x * BLOCK + threadIdx.x;
     if (i >= n) return;
     const Vec4<float> pi = ld4(pos + i);
     const Vec4<float> vi = ld4(vel + i);
@@ -170,61 +207,53 @@ __global__ void __launch_bounds__(128, 8) k_forces_mixed(
     const SceneDev sc = load_scene(scenes, wbits(pi.w));
     int cx, cy, cz;
     hash_cell<float>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
-    const float qi = ai.z;
+    const float qs = ai.z * Q_SCALE;
     float fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
-    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
-    const int xl = cx > 0 ? cx - 1 : 0, xh = cx + 1 < X ? cx + 1 : X - 1;
-    int r = 0;
+    using St = Stencil<RAD>;
 #pragma unroll 1
-    for (int dz = -1; dz <= 1; dz++) {
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; dy++, r++) {
-            const int z = cz + dz, y = cy + dy;
-            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
-            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
-            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
-            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
-            const uint32_t nw = (je - jb + 31) / 32;
-            for (uint32_t w = 0; w < nw; w++) {
-                const uint32_t cb = jb + 32 * w;
-                uint32_t m = 0;
-                if (w < (uint32_t) MASK_WORDS) {
-                    m = __ldg(masks + (size_t) (r * MASK_WORDS + w) * n + i);
-                } else {  // beyond the recorded chunks: test the candidates here
-                    const uint32_t ce = min(je, cb + 32u);
-                    for (uint32_t j = ce; j-- > cb;) {
-                        float x, yy, zz;
-                        code_delta(gi, __ldg(gpos + j), x, yy, zz);
-                        m = (m << 1) | (h2_minus_r2<float>(x, yy, zz, QH2) > 0.0f ? 1u : 0u);
-                    }
+    for (int r = 0; r < St::ROWS; r++) {
+        uint32_t jb, je;
+        if (!stencil_row<RAD>(sc, start, cx, cy, cz, r, jb, je)) continue;
+        if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
+        const uint32_t nw = (je - jb + 31) / 32;
+        // the row's recorded words loaded together at the start of the row
+        const uint32_t *mr = masks + (size_t) (r * St::WORDS) * n + i;
+        uint32_t wr[St::WORDS];
+#pragma unroll
+        for (int k = 0; k < St::WORDS; k++) wr[k] = nw > (uint32_t) k ? __ldg(mr + k * (size_t) n) : 0u;
+        for (uint32_t w = 0; w < nw; w++) {
+            const uint32_t cb = jb + 32 * w;
+            uint32_t m = 0;
+            if (w < (uint32_t) St::WORDS) {
+                m = wr[0];
+#pragma unroll
+                for (int k = 1; k < St::WORDS; k++) m = w == (uint32_t) k ? wr[k] : m;
+            } else {  // beyond the recorded chunks: test the candidates here
+                const uint32_t ce = min(je, cb + 32u);
+                for (uint32_t j = ce; j-- > cb;) {
+                    float x, yy, zz;
+                    code_delta(gi, __ldg(gpos + j), x, yy, zz);
+                    m = (m << 1) | (h2_minus_r2<float>(x, yy, zz, QH2) > 0.0f ? 1u : 0u);
                 }
-                while (m) {
-                    const uint32_t j = cb + (uint32_t) (__ffs(m) - 1);
-                    m &= m - 1;
-                    if (j == i || !sph_check(j < je, CHK_NEIGHBOUR)) continue;
-                    float dx, dy_, dz_, vjx, vjy, vjz;
-                    code_delta(gi, __ldg(gpos + j), dx, dy_, dz_);
-                    unpack_half3(__ldg(gvel + j), vjx, vjy, vjz);
-                    const float2 qa = __ldg(reinterpret_cast<const float2 *>(aux + j) + 1);
-                    // at least one unit apart: two particles sharing a code (closer than the
-                    // 5.6 um resolution) get no pressure direction rather than a 0/0
-                    const float r2 = fmaxf(dx * dx + dy_ * dy_ + dz_ * dz_, 1.0f);
-                    const float rinv = rsqrtf(r2);
-                    const float hr = QUNITS - r2 * rinv;
-                    const float wgt = (qi + qa.x) * (mc.spiky_q * hr * hr * rinv);
-                    fpx += wgt * dx;
-                    fpy += wgt * dy_;
-                    fpz += wgt * dz_;
-                    const float l = mc.visc_q * hr * qa.y;
-                    fvx += (vjx - vi.x) * l;
-                    fvy += (vjy - vi.y) * l;
-                    fvz += (vjz - vi.z) * l;
-                }
+            }
+            if (i - cb < 32u) m &= ~(1u << (i - cb));  // the particle itself
+            while (m) {
+                const uint32_t j0 = cb + (uint32_t) (__ffs(m) - 1);
+                m &= m - 1;
+                const bool two = m != 0;
+                const uint32_t j1 = two ? cb + (uint32_t) (__ffs(m) - 1) : j0;
+                m &= m - 1;
+                if (!sph_check(j0 < je && j1 < je, CHK_NEIGHBOUR)) continue;
+                const uint4 r0 = __ldg(rec + j0), r1 = __ldg(rec + j1);
+                mixed_pair(gi, vi, qs, r0, mc, fpx, fpy, fpz, fvx, fvy, fvz);
+                if (two) mixed_pair(gi, vi, qs, r1, mc, fpx, fpy, fpz, fvx, fvy, fvz);
             }
         }
     }
+    // the scene record again rather than kept live across the pair loop (fewer registers)
+    const SceneDev sc2 = load_scene(scenes, wbits(pi.w));
     float ax, ay, az;
-    accel_of<float>(pi, vi, ai.x, sc, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, ax, ay, az);
+    accel_of<float>(pi, vi, ai.x, sc2, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, ax, ay, az);
     // x' = x + (v dt + (a dt) dt) with x = hi + lo carried by TwoSum; v' = increment / dt
     const Vec4<float> li = ld4(lo_s + i);
     const float dt = c.dt;
@@ -240,8 +269,8 @@ __global__ void __launch_bounds__(128, 8) k_forces_mixed(
     st4(vel_out + i, Vec4<float>{__fdiv_rn(ix, dt), __fdiv_rn(iy, dt), __fdiv_rn(iz, dt), vi.w});
     if (acc_out) st4(acc_out + i, Vec4<float>{ax, ay, az, 0.0f});
     int qx, qy, qz;
-    const uint32_t cell = hash_cell<float>(sc, hx, hy, hz, c, qx, qy, qz);
-    atomicAdd(count + cell, 1u);
+    const uint32_t cell = hash_cell<float>(sc2, hx, hy, hz, c, qx, qy, qz);
+    count_add(count, cell);
     cid_out[i] = make_uint2(cell, wbits(vi.w));
 }
 
@@ -293,28 +322,57 @@ cudaError_t mixed_permute(const DevBufs &b, uint32_t n, Consts<float> c, MixCons
     k_rank_permute_mixed<<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.start, b.tmp, (const Vec4<float> *) b.pos_u,
                                                        (const Vec4<float> *) b.lo_u, (const Vec4<float> *) b.vel_u,
                                                        b.scenes, c, mc, (Vec4<float> *) b.pos_s,
-                                                       (Vec4<float> *) b.lo_s, (Vec4<float> *) b.vel_s, b.gpos, b.gvel);
+                                                       (Vec4<float> *) b.lo_s, (Vec4<float> *) b.vel_s, b.gpos);
     return cudaGetLastError();
 }
 
-cudaError_t mixed_density(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, cudaStream_t st)
+cudaError_t mixed_density(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, int cell_mult,
+                          cudaStream_t st)
 {
     if (!n) return cudaSuccess;
     // blocks of 128: the SMs finish the dense and sparse regions more evenly than with 256
-    k_density_mixed<<<nblk(n, 128), 128, 0, st>>>((const Vec4<float> *) b.pos_s, b.gpos, (Vec4<float> *) b.aux,
-                                                  b.start, b.scenes, n, c, mc, b.masks);
+    if (cell_mult == 2)
+        k_density_mixed<2><<<nblk(n, 128), 128, 0, st>>>((const Vec4<float> *) b.pos_s, b.gpos, (Vec4<float> *) b.aux,
+                                                         b.start, b.scenes, n, c, mc, b.masks,
+                                                         (const Vec4<float> *) b.vel_s, (uint4 *) b.frec);
+    else
+        k_density_mixed<1><<<nblk(n, 128), 128, 0, st>>>((const Vec4<float> *) b.pos_s, b.gpos, (Vec4<float> *) b.aux,
+                                                         b.start, b.scenes, n, c, mc, b.masks,
+                                                         (const Vec4<float> *) b.vel_s, (uint4 *) b.frec);
     return cudaGetLastError();
 }
 
-cudaError_t mixed_forces(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, bool record_acc,
-                         cudaStream_t st)
+template <int MINB, int BLOCK, int RAD>
+static void launch_forces_mixed(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, bool record_acc,
+                                cudaStream_t st)
 {
-    if (!n) return cudaSuccess;
-    k_forces_mixed<<<nblk(n, 128), 128, 0, st>>>(
+    k_forces_mixed<MINB, BLOCK, RAD><<<nblk(n, BLOCK), BLOCK, 0, st>>>(
         (const Vec4<float> *) b.pos_s, (const Vec4<float> *) b.lo_s, (const Vec4<float> *) b.vel_s,
-        (const Vec4<float> *) b.aux, b.gpos, b.gvel, b.start, b.scenes, b.obstacles, n, c, mc, b.masks,
+        (const Vec4<float> *) b.aux, b.gpos, (const uint4 *) b.frec, b.start, b.scenes, b.obstacles, n, c, mc, b.masks,
         (Vec4<float> *) b.pos_u, (Vec4<float> *) b.lo_u, (Vec4<float> *) b.vel_u,
         record_acc ? (Vec4<float> *) b.acc : nullptr, b.cid_u, b.count);
+}
+
+template <int RAD>
+static void mixed_forces_rad(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, bool record_acc,
+                             int variant, cudaStream_t st)
+{
+    // variants: blocks of 128 threads at most 64 (0) or 48 (1) registers, blocks of 256 threads
+    // with no cap (2) or at 48 registers (3); every variant computes the same bits
+    switch (variant) {
+    case 1: launch_forces_mixed<10, 128, RAD>(b, n, c, mc, record_acc, st); break;
+    case 2: launch_forces_mixed<1, 256, RAD>(b, n, c, mc, record_acc, st); break;
+    case 3: launch_forces_mixed<5, 256, RAD>(b, n, c, mc, record_acc, st); break;
+    default: launch_forces_mixed<8, 128, RAD>(b, n, c, mc, record_acc, st); break;
+    }
+}
+
+cudaError_t mixed_forces(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, bool record_acc, int variant,
+                         int cell_mult, cudaStream_t st)
+{
+    if (!n) return cudaSuccess;
+    if (cell_mult == 2) mixed_forces_rad<2>(b, n, c, mc, record_acc, variant, st);
+    else mixed_forces_rad<1>(b, n, c, mc, record_acc, variant, st);
     return cudaGetLastError();
 }
 

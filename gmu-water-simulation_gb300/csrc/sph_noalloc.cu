@@ -4,9 +4,14 @@
 // already handed its GPU memory to its own pool allocator, or a per-frame callback in a
 // real-time loop, where cudaMalloc/cudaFree would synchronise the device and stall the frame.
 // The caller passes device arrays for the positions and for every output; the kernels'
-// working memory (per-cell counts and cursors, per-particle slot ids, scan block sums) lives
-// in one file-scope device array of fixed size, reserved when the library's module is loaded
-// and held by every GPU that loads it until the process exits.
+// working memory (per-cell counts and cursors, per-particle slot ids, scan block sums, the list
+// of crowded cells) lives in one file-scope device array of fixed size. The array belongs to
+// the library's device code: CUDA creates it on a device when that code is loaded there, which
+// under lazy module loading (the default) is the first call on that device. That first call
+// also looks up the array's device address, so it belongs in the caller's setup: before its
+// pool allocator takes the GPU's memory and before any stream capture. Every GPU that has run
+// a call holds the array until the process exits. cudaDeviceReset is not supported between
+// calls: the address looked up by the first call would then be stale.
 //
 // Limits: at most kMaxParticles particles and kMaxCells grid cells per call (about 12 MiB of
 // scratch). Calls share the scratch array, which keeps the previous call's contents: each
@@ -14,9 +19,11 @@
 // different streams, or from different host threads) race on it and must not be issued.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <mutex>
 
 #include "../../include/sph_cuda.h"
+#include "sph_device.cuh"
 #include "sph_internal.h"
 
 namespace sph {
@@ -25,8 +32,9 @@ namespace {
 constexpr uint32_t kMaxParticles = 1u << 20;
 constexpr uint32_t kMaxCells = 1u << 20;
 constexpr uint32_t kMaxBlocks = kMaxCells / kScanTile + 1;  // scan block sums
-// counts | cursors | slot ids | scan block sums, as 32-bit words
-constexpr size_t kScratchWords = (size_t) kMaxCells + kMaxCells + kMaxParticles + kMaxBlocks;
+constexpr size_t kBigWords = big_words(kMaxParticles);       // crowded-cell list
+// counts | cursors | slot ids | scan block sums | crowded cells, as 32-bit words
+constexpr size_t kScratchWords = (size_t) kMaxCells + kMaxCells + kMaxParticles + kMaxBlocks + kBigWords;
 
 __device__ __align__(256) uint32_t g_grid_scratch[kScratchWords];
 
@@ -66,12 +74,46 @@ __global__ void __launch_bounds__(256) k_rank_ids(const uint32_t *__restrict__ c
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t c = cell[i], b = start[c], e = start[c + 1];
-    uint32_t r = 0;
-    for (uint32_t k = b; k < e; k++) r += slot_ids[k] < i ? 1u : 0u;
-    order[b + r] = i;
+    const uint32_t dst = b + rank_in_cell(slot_ids, b, e, i);
+    if (sph_check(dst < e && e <= n, CHK_SORT)) order[dst] = i;
 }
 
 }  // namespace
+
+// The reference's grid of n particles (float xyz, id order) in a box of res cells per axis (cells
+// of size h, linear index x + y*X + z*X*Y): the cell of every particle, the cell starts and the
+// ids in ascending (cell, id) order, with the working memory g (counts, cursors, slot ids, scan
+// block sums, crowded-cell list) supplied by the caller.
+cudaError_t ref_grid_build(const float *xyz, uint32_t n, int3 res, float3 half, float h, uint32_t *out_cell,
+                           uint32_t *out_start, uint32_t *out_order, const GridScratch &g, cudaStream_t st)
+{
+    const uint64_t ncells = (uint64_t) res.x * (uint64_t) res.y * (uint64_t) res.z;
+    DevBufs b{};
+    b.count = g.count;
+    b.cursor = g.cursor;
+    b.tmp = g.tmp;
+    b.bsum = g.bsum;
+    b.big = g.big;
+    b.start = out_start;
+    // counts must start at zero: the previous call's values remain in the array
+    cudaError_t e = cudaMemsetAsync(b.count, 0, 4 * ncells, st);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = (unsigned) ((n + 255) / 256);
+    if (n) k_hash_plain_xyz<<<blocks, 256, 0, st>>>(xyz, n, half, res, 1.0f / h, (double) h, out_cell, b.count);
+    e = Launch<float>::scan(b, (uint32_t) ncells, st);  // starts; cursors = starts; counts back to 0
+    if (e == cudaSuccess && n) {
+        k_slot_ids<<<blocks, 256, 0, st>>>(out_cell, n, b.cursor, b.tmp);
+        e = launch_sort_big(b.start, b.tmp, b.big, st);
+        if (e == cudaSuccess) {
+            k_rank_ids<<<blocks, 256, 0, st>>>(out_cell, n, b.start, b.tmp, out_order);
+            e = cudaGetLastError();
+        }
+    }
+    return e;
+}
+
+SPH_CHECK_ACCESSOR(check_flags_noalloc)
+
 }  // namespace sph
 
 using namespace sph;
@@ -80,15 +122,19 @@ using namespace sph;
 extern "C" int sph_grid_build_noalloc(const float *xyz, uint32_t n, const float box[3], float h, uint32_t *out_cell,
                                       uint32_t *out_start, uint32_t *out_order, void *stream)
 {
-    if (!box || !(h > 0) || !out_start) return SPH_ERR_ARG;
+    if (!box || !(h > 0) || !std::isfinite(h) || !out_start) return SPH_ERR_ARG;
     if (n && (!xyz || !out_cell || !out_order)) return SPH_ERR_ARG;
-    for (int a = 0; a < 3; a++)
-        if (!(box[a] > 0)) return SPH_ERR_ARG;
-    int3 res;
-    res.x = (int) ceilf(box[0] / h);
-    res.y = (int) ceilf(box[1] / h);
-    res.z = (int) ceilf(box[2] / h);
-    const uint64_t ncells = (uint64_t) res.x * res.y * res.z;
+    // cells per axis as the context computes them (float quotient, then ceil), checked against
+    // the scratch limit before the conversion to int so that no huge or infinite quotient is cast
+    int r3[3];
+    for (int a = 0; a < 3; a++) {
+        if (!(box[a] > 0) || !std::isfinite(box[a])) return SPH_ERR_ARG;
+        const float q = ceilf(box[a] / h);
+        if (!(q <= (float) kMaxCells)) return SPH_ERR_CAPACITY;  // also an infinite quotient
+        r3[a] = (int) q;
+    }
+    const int3 res = make_int3(r3[0], r3[1], r3[2]);
+    const uint64_t ncells = (uint64_t) res.x * (uint64_t) res.y * (uint64_t) res.z;
     if (n > kMaxParticles || ncells > kMaxCells) return SPH_ERR_CAPACITY;  // beyond the fixed scratch
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SPH_ERR_CUDA;
@@ -103,25 +149,13 @@ extern "C" int sph_grid_build_noalloc(const float *xyz, uint32_t n, const float 
         }
         scratch = g_scratch_ptr[dev];
     }
-    cudaStream_t st = (cudaStream_t) stream;
-    DevBufs b{};
-    b.count = scratch;
-    b.cursor = scratch + kMaxCells;
-    b.tmp = scratch + 2 * (size_t) kMaxCells;
-    b.bsum = scratch + 2 * (size_t) kMaxCells + kMaxParticles;
-    b.start = out_start;
-    // counts must start at zero: the previous call's values remain in the array
-    if (cudaMemsetAsync(b.count, 0, 4 * ncells, st) != cudaSuccess) return SPH_ERR_CUDA;
-    const unsigned blocks = (unsigned) ((n + 255) / 256);
-    if (n) {
-        const float3 half = make_float3(box[0] / 2.0f, box[1] / 2.0f, box[2] / 2.0f);
-        k_hash_plain_xyz<<<blocks, 256, 0, st>>>(xyz, n, half, res, 1.0f / h, (double) h, out_cell, b.count);
-    }
-    cudaError_t e = Launch<float>::scan(b, (uint32_t) ncells, st);  // starts; cursors = starts; counts back to 0
-    if (e == cudaSuccess && n) {
-        k_slot_ids<<<blocks, 256, 0, st>>>(out_cell, n, b.cursor, b.tmp);
-        k_rank_ids<<<blocks, 256, 0, st>>>(out_cell, n, b.start, b.tmp, out_order);
-        e = cudaGetLastError();
-    }
+    GridScratch g;
+    g.count = scratch;
+    g.cursor = scratch + kMaxCells;
+    g.tmp = scratch + 2 * (size_t) kMaxCells;
+    g.bsum = scratch + 2 * (size_t) kMaxCells + kMaxParticles;
+    g.big = g.bsum + kMaxBlocks;
+    const float3 half = make_float3(box[0] / 2.0f, box[1] / 2.0f, box[2] / 2.0f);
+    const cudaError_t e = ref_grid_build(xyz, n, res, half, h, out_cell, out_start, out_order, g, (cudaStream_t) stream);
     return e == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }

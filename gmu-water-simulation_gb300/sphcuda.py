@@ -31,7 +31,8 @@ SPH_FLAG_PROFILE, SPH_FLAG_RECORD_ACC, SPH_FLAG_ALL_PAIRS = 1, 2, 4
 # every symbol the header declares
 EXPORTS = (
     "sph_params_default", "sph_create", "sph_batch_create", "sph_memory_required", "sph_debug_check", "sph_destroy", "sph_last_error", "sph_device_name",
-    "sph_stream", "sph_set_variant", "sph_get_variant", "sph_autotune", "sph_set_online_tuning", "sph_grid_build_noalloc",
+    "sph_stream", "sph_set_variant", "sph_get_variant", "sph_set_cell_multiple", "sph_get_cell_multiple", "sph_autotune",
+    "sph_set_online_tuning", "sph_grid_build_noalloc",
     "sph_upload", "sph_append", "sph_emit_fountain", "sph_set_gravity", "sph_step", "sph_pass_grid", "sph_pass_density",
     "sph_pass_forces", "sph_pass_times", "sph_get_counts", "sph_num_scenes", "sph_num_particles",
     "sph_get_resolution", "sph_download", "sph_download_f64", "sph_handoff_async", "sph_handoff_ready",
@@ -94,6 +95,8 @@ def load(path=None):
         "sph_stream": (vp, [vp]),
         "sph_set_variant": (i32, [vp, i32, i32]),
         "sph_get_variant": (i32, [vp, ip]),
+        "sph_set_cell_multiple": (i32, [vp, i32]),
+        "sph_get_cell_multiple": (i32, [vp]),
         "sph_autotune": (i32, [vp, i32]),
         "sph_set_online_tuning": (i32, [vp, i32]),
         "sph_grid_build_noalloc": (i32, [vp, u32, fp, f, vp, vp, vp, vp]),
@@ -332,12 +335,22 @@ class SphContext:
         self._ck(load().sph_get_variant(self.h, _p(v, ctypes.c_int32)))
         return int(v[0]), int(v[1])
 
+    def set_cell_multiple(self, m):
+        """Step grid of cells h / m (1: the reference's cells; 2: cells of h/2, 125-cell stencil)."""
+        self._ck(load().sph_set_cell_multiple(self.h, m))
+
+    def cell_multiple(self):
+        m = load().sph_get_cell_multiple(self.h)
+        if m < 0:
+            self._ck(m)
+        return m
+
     def autotune(self, reps=3):
         self._ck(load().sph_autotune(self.h, reps))
         return self.variant()
 
     def set_online_tuning(self, period):
-        """Re-time the mask-driven force variants every `period` steps (0 = off)."""
+        """Re-time the force variants every `period` steps (0 = off)."""
         self._ck(load().sph_set_online_tuning(self.h, period))
 
     def debug_check(self):
@@ -566,17 +579,22 @@ class CCUDAParticleSimulator:
         self.ctx.append(0, pts, vel)
         self.m_particlesCount += per
 
+    def _pass_time(self, k):
+        # each pass returns its own milliseconds (0 when profiling is off): a profiled pass call
+        # waits for its work, so its time is known when it returns
+        return float(self.ctx.pass_times()[k]) if self.flags & SPH_FLAG_PROFILE else 0.0
+
     def updateGrid(self):
         self.ctx.pass_grid()
-        return 0.0
+        return self._pass_time(0)
 
     def updateDensityPressure(self):
         self.ctx.pass_density()
-        return 0.0
+        return self._pass_time(1)
 
     def updateForces(self):
         self.ctx.pass_forces()
-        return 0.0
+        return self._pass_time(2)
 
     def updateCollisions(self):
         return 0.0  # fused into the force pass
@@ -587,13 +605,10 @@ class CCUDAParticleSimulator:
     def step(self):
         try:
             self._generateParticles()
-            self.updateGrid()
-            self.updateDensityPressure()
-            self.updateForces()
-            self.updateCollisions()
-            self.integrate()
+            t = [self.updateGrid(), self.updateDensityPressure(), self.updateForces(), self.updateCollisions(),
+                 self.integrate()]
             if self.flags & SPH_FLAG_PROFILE:
-                self._times = self.ctx.pass_times()
+                self._times = np.array(t)
                 if self.totalIteration % self.eventLoggerStride == 0:
                     self.events.append(ProfilingEvent(self.totalIteration, self.getFps(), *self._times))
             self.totalIteration += 1

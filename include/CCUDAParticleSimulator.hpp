@@ -7,8 +7,8 @@
 // the reference's order (:116-144); the pass methods return milliseconds (0 when profiling is
 // off, and 0 for updateCollisions/integrate, which are fused into updateForces); a failing
 // step stops the simulator and reports through the errorOccured callback, as
-// CGPUBaseParticleSimulator::step does (src/CGPUBaseParticleSimulator.cpp:28-37). The Qt
-// adapter in INTEGRATION.md wraps the same calls in a CBaseParticleSimulator subclass.
+// CGPUBaseParticleSimulator::step does (src/CGPUBaseParticleSimulator.cpp:28-37). A Qt
+// subclass of CBaseParticleSimulator makes the same calls in the same order.
 #ifndef CCUDAPARTICLESIMULATOR_HPP
 #define CCUDAPARTICLESIMULATOR_HPP
 
@@ -188,25 +188,29 @@ public:
         check(sph_download(m_ctx, xyz.data(), vel.data(), rho.data(), nullptr, nullptr));
     }
 
+    // each pass returns its own milliseconds (0 when profiling is off): with profiling on, a
+    // pass call waits for its work and its time is read right after it
+    double passTime(int k)
+    {
+        if (!m_profiling) return 0.0;
+        double ms[5];
+        check(sph_pass_times(m_ctx, ms));
+        return ms[k];
+    }
     double updateGrid()
     {
         check(sph_pass_grid(m_ctx));
-        return 0.0;
+        return passTime(0);
     }
     double updateDensityPressure()
     {
         check(sph_pass_density(m_ctx));
-        return 0.0;
+        return passTime(1);
     }
     double updateForces()
     {
         check(sph_pass_forces(m_ctx));
-        if (!m_profiling) return 0.0;
-        double ms[5];
-        check(sph_pass_times(m_ctx, ms));
-        m_last[0] = ms[0];  // the grid and density passes are timed with the step's events
-        m_last[1] = ms[1];
-        return ms[2];
+        return passTime(2);
     }
     double updateCollisions() { return 0.0; }  // fused into updateForces
     double integrate() { return 0.0; }         // fused into updateForces

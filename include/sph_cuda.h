@@ -175,9 +175,11 @@ int sph_pass_grid(sph_ctx *ctx);
 int sph_pass_density(sph_ctx *ctx);
 int sph_pass_forces(sph_ctx *ctx);
 
-/* Milliseconds of the last step's passes (grid, density, forces, collisions, integrate),
- * the fields of sProfilingEvent (include/SProfilingEvent.h:8-31). Needs SPH_FLAG_PROFILE;
- * collisions and integrate are fused into forces and report 0. */
+/* Milliseconds of the latest passes (grid, density, forces, collisions, integrate), the
+ * fields of sProfilingEvent (include/SProfilingEvent.h:8-31). Needs SPH_FLAG_PROFILE; with it
+ * each sph_pass_* call waits for its own work, so its time is here when the call returns (the
+ * reference's profiled passes each return their own duration). Collisions and integrate are
+ * fused into forces and report 0. */
 int sph_pass_times(sph_ctx *ctx, double ms[5]);
 
 /* Launch variants of the two neighbour passes. Every variant computes the same bits; only
@@ -193,27 +195,44 @@ int sph_pass_times(sph_ctx *ctx, double ms[5]);
  *            iteration (5 capped at 64); 7 is 6 reading each neighbour from one packed 32-byte
  *            force record written by the density pass; 8 and 9 are 7 capped at 48 and 40
  *            registers (5 and 6 blocks of 256 per SM); 10 and 11 are 9 and 8 launched in
- *            blocks of 128 threads (12 and 10 per SM). SPH_ERR_ARG for other numbers. */
+ *            blocks of 128 threads (12 and 10 per SM). SPH_ERR_ARG for other numbers.
+ * The mixed form has one density pass (density_variant 0) and force variants 0..3: blocks of
+ * 128 threads at up to 64 or 48 registers, blocks of 256 with no cap or 48 registers. On cells
+ * of h/2 (sph_set_cell_multiple) the plain form runs density 0 with force variants 7..11. */
 int sph_set_variant(sph_ctx *ctx, int32_t density_variant, int32_t forces_variant);
 int sph_get_variant(const sph_ctx *ctx, int32_t out[2]);
 
-/* Autotuner: one step in which every (density, forces) variant pair is timed on the current
- * state (both passes re-run from the same sorted inputs), the fastest pair is kept, and the
+/* Cell multiple of the step's grid: 1 = the reference's cells of size h and 27-cell stencil
+ * (src/CBaseParticleSimulator.cpp:27-31, resources/kernels/sph_grid.cl:124-170); 2 = cells of
+ * h/2 with a 125-cell stencil (5 rows of 5 cells in each of 5 planes), which covers 15.6 h^3
+ * around a particle instead of 27 h^3, so the density pass tests about 42% fewer candidates.
+ * The method and its results are the same within rounding (the candidates are summed in another
+ * order). The plain FP32 and mixed forms only (SPH_ERR_UNSUPPORTED for FP64 and all-pairs);
+ * between steps only (SPH_ERR_STATE between passes). sph_get_grid still reports the reference's
+ * grid of cells of size h. sph_get_cell_multiple returns the current multiple (or SPH_ERR_ARG).
+ * The autotuner chooses the multiple with the variants. */
+int sph_set_cell_multiple(sph_ctx *ctx, int32_t cell_multiple);
+int sph_get_cell_multiple(const sph_ctx *ctx);
+
+/* Autotuner: one step in which every (cell multiple, density, forces) choice is timed on the
+ * current state (per cell multiple the grid pass once, then both neighbour passes re-run from the
+ * same sorted inputs per variant pair), the fastest grid + density + forces is kept, and the
  * choice is written to the cache file (SPH_TUNE_CACHE, else $HOME/.cache/sph_gb300/tune.txt)
- * under the device name, precision and particle-count
- * bucket (floor(log2 n)). sph_upload applies a cached choice for its bucket. The simulation
- * advances by exactly one step; reps = timed repetitions per variant (>= 1). */
+ * under the device name, precision and particle-count bucket (floor(log2 n)). sph_upload applies
+ * a cached choice for its bucket. The simulation advances by exactly one step; reps = timed
+ * repetitions per variant (>= 1). */
 int sph_autotune(sph_ctx *ctx, int32_t reps);
 
 /* Online tuning of the force variant for a state that changes over a run (a collapsing dam
  * break packs ~4x more neighbours per particle after a few hundred steps than at the start,
  * and the fastest variant changes with it). Every `period` steps (sph_step or the pass
- * calls), one real step runs with each of the record-reading force variants 7, 9, 10 and 11,
- * timed with events on the context's stream (one host synchronisation per trial step), and the
- * fastest is kept until the next trial. All of them compute the same bits, so the results do
- * not depend on the choice. Applies while the current force variant is mask-driven (3..11).
- * period 0 turns it off (the default); otherwise period >= 4. Not for mixed or all-pairs
- * contexts (SPH_ERR_STATE). */
+ * calls), one real step runs with each of the record-reading force variants 7, 9, 10 and 11
+ * (the mixed form: its variants 0..3), timed with events on the context's stream (one host
+ * synchronisation per trial step), and the fastest is kept until the next trial. All of them
+ * compute the same bits, so the results do not depend on the choice; the cell multiple stays.
+ * Applies while the current force variant is mask-driven (3..11, or any mixed variant).
+ * period 0 turns it off (the default); otherwise period >= 4. Not for all-pairs contexts
+ * (SPH_ERR_STATE). */
 int sph_set_online_tuning(sph_ctx *ctx, int32_t period);
 
 /* Particle count of every scene (n_scenes entries). */
@@ -285,11 +304,15 @@ int sph_stats(sph_ctx *ctx, uint32_t scene, double out[8]);
  *   out_order  n: particle ids in ascending (cell, id) order
  * The cells and order equal the grid that sph_pass_grid builds for the same positions and h.
  * Working memory is one fixed device array of about 12 MiB inside this library, held by every
- * GPU that loads it until the process exits, so n and X*Y*Z are each limited to 1,048,576;
- * larger requests return SPH_ERR_CAPACITY. The first call on a device looks up that array's
- * device address (make that first call before any stream capture). All calls share the array:
- * calls whose work overlaps on the GPU race on it and must not be issued. Work is queued on
- * stream (a cudaStream_t; NULL = the legacy default stream); returns a status code only. */
+ * GPU that has run a call until the process exits, so n and X*Y*Z are each limited to 1,048,576;
+ * larger requests return SPH_ERR_CAPACITY, and a non-finite box or h SPH_ERR_ARG. The first call
+ * on a device is its setup: CUDA creates the array there when the library's device code is
+ * loaded (under lazy loading, at that call), and the call looks up the array's device address.
+ * Make it at the caller's setup, before its pool allocator takes the GPU's memory and before any
+ * stream capture; later calls allocate nothing. cudaDeviceReset between calls is not supported
+ * (the address found at setup would be stale). All calls share the array: calls whose work
+ * overlaps on the GPU race on it and must not be issued. Work is queued on stream (a
+ * cudaStream_t; NULL = the legacy default stream); returns a status code only. */
 int sph_grid_build_noalloc(const float *xyz, uint32_t n, const float box[3], float h, uint32_t *out_cell,
                            uint32_t *out_start, uint32_t *out_order, void *stream);
 

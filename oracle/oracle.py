@@ -42,19 +42,24 @@ def build(force=False):
 
 # The reference's own OpenCL kernels compiled for the CPU (oracle/ref_cl): built only where the
 # reference tree is present, into oracle/_ref/ (not committed, not usable on another machine).
-REF_KERNELS = os.environ.get("SPH_REF_KERNELS", "/root/reference/resources/kernels")
+# The kernels' directory (resources/kernels of the reference tree) comes from the caller or from
+# SPH_REF_KERNELS; without either, an already built library is used if there is one.
 REF_DIR = os.path.join(HERE, "_ref")
 REF_LIB = os.path.join(REF_DIR, "librefcl.so")
 _ref = None
 
 
-def build_ref(force=False):
-    """Compile oracle/ref_cl/ref_cl.cpp, which includes sph_common.cl and sph_grid.cl from the
-    reference tree where they lie, into oracle/_ref/librefcl.so. Returns the path, or None when
-    the reference tree is absent."""
-    srcs = [os.path.join(REF_KERNELS, f) for f in ("sph_common.cl", "sph_grid.cl", "sph_brute.cl")]
+def build_ref(kernels_dir=None, force=False):
+    """Compile oracle/ref_cl/ref_cl.cpp, which includes sph_common.cl, sph_grid.cl and
+    sph_brute.cl from kernels_dir (default: $SPH_REF_KERNELS) where they lie, into
+    oracle/_ref/librefcl.so. Returns the path, or None when neither the kernels nor a built
+    library are present."""
+    kernels_dir = kernels_dir or os.environ.get("SPH_REF_KERNELS")
+    if not kernels_dir:
+        return REF_LIB if os.path.exists(REF_LIB) else None
+    srcs = [os.path.join(kernels_dir, f) for f in ("sph_common.cl", "sph_grid.cl", "sph_brute.cl")]
     if not all(os.path.exists(f) for f in srcs):
-        return None
+        return REF_LIB if os.path.exists(REF_LIB) else None
     here = os.path.join(HERE, "ref_cl")
     deps = srcs + [os.path.join(here, f) for f in ("ref_cl.cpp", "cl_shim.h")]
     if force or not os.path.exists(REF_LIB) or os.path.getmtime(REF_LIB) < max(os.path.getmtime(f) for f in deps):
@@ -62,7 +67,7 @@ def build_ref(force=False):
         tmp = REF_LIB + ".tmp"
         subprocess.check_call([os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC", "-shared",
                                "-ffp-contract=off", "-Wno-unknown-pragmas", "-Wno-unused-value",
-                               "-Wno-unused-variable", "-I", here, "-I", REF_KERNELS,
+                               "-Wno-unused-variable", "-I", here, "-I", kernels_dir,
                                os.path.join(here, "ref_cl.cpp"), "-o", tmp])
         os.replace(tmp, REF_LIB)
     return REF_LIB

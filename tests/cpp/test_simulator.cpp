@@ -46,6 +46,8 @@ int main(int argc, char **argv)
         for (int k = 0; k < 17; k++) sim.step();
         CHECK(sim.events.size() == 3 && sim.events[2].iteration == 20);
         CHECK(sim.events[1].updateForces > 0 && sim.events[2].fps > 0);
+        // every pass returns its own time from its own call
+        CHECK(sim.events[1].updateGrid > 0 && sim.events[1].updateDensityPressure > 0);
         CHECK(sim.exportLogs(logdir, "GPU CUDA", "Dam break"));
         FILE *f = std::fopen((logdir + "/Dam break_0.4.csv").c_str(), "r");
         CHECK(f != nullptr);

@@ -41,7 +41,8 @@ def scene(kind):
 
 def main():
     O.build()
-    if O.build_ref() is None:
+    root = os.environ.get("SPH_REFERENCE_ROOT", "/root/reference")  # the reference tree
+    if O.build_ref(os.path.join(root, "resources", "kernels")) is None:
         raise SystemExit("the reference tree is not present: nothing to generate")
     out = {}
     for name, box, g, kind, steps in CASES:

@@ -37,4 +37,33 @@ def test_byte_model_matches_the_documented_totals():
         ab = bench.alg_bytes(N, C, 4, v)
         assert ab["density"] == 116 * N + 4 * C and ab["forces"] == 156 * N + 12 * C
         assert sum(ab.values()) == 360 * N + 48 * C
-        assert ("k_forces", v) in bench.TRAFFIC and ("k_density", v) in bench.TRAFFIC
+    assert set(bench.TRAFFIC) == {"k_forces", "k_density"} and set(bench.ISSUE) == set(bench.TRAFFIC)
+
+
+def test_reference_arm_loads_no_product_library():
+    """The reference arm builds its scene from the oracle's restatement and times only the
+    oracle: the product library is never mapped into its process."""
+    code = ("import sys, runpy; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '2', "
+            "'--threads', '2']\n"
+            "try:\n    runpy.run_path('bench.py', run_name='__main__')\nexcept SystemExit:\n    pass\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print('PRODUCT_MAPPED' if 'libsph_gb300' in maps else 'PRODUCT_NOT_MAPPED')\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = r.stdout.strip().splitlines()
+    assert out[-1] == "PRODUCT_NOT_MAPPED"
+    line = json.loads(out[-2])
+    assert line["warmup"] == 2  # the requested warm-up, not a capped one
+
+
+def test_compulsory_bytes():
+    """The roofline's algorithmic bytes: density 24 B, forces 72 B per particle, the step 196 B per
+    particle plus 12 B per cell (plain FP32)."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    N, C = 1_000_000, bench.grid_cells(bench.BOX)
+    cb = bench.compulsory_bytes(N, C)
+    assert cb == {"density": 24 * N, "forces": 72 * N, "step": 196 * N + 12 * C}
+    assert bench.timed_steps(20, 500) == list(range(0, 500, 25))
+    assert bench.timed_steps(500, 500) == list(range(500))

@@ -23,7 +23,7 @@ rng = np.random.default_rng(11)
 clump = (rng.random((1500, 3)) * 0.12 - 0.06).astype(np.float32)
 lattice = sphcuda.dam_break_scene((12, 12, 12), (1.0, 1.0, 0.5), 2)
 g = (0.0, -9.81, 0.0)
-variants = [(d, f) for d in (0, 1, 2, 4) for f in (0, 1, 2)] + [(0, f) for f in range(3, 10)]
+variants = [(d, f) for d in (0, 1, 2, 4) for f in (0, 1, 2)] + [(0, f) for f in range(3, 12)]
 for name, box, pos in (("clump", (0.5, 0.5, 0.5), clump), ("lattice", (1.0, 1.0, 0.5), lattice)):
     for dv, fv in variants:
         ctx = sphcuda.SphContext(box, pos.shape[0], gravity=g)
@@ -45,6 +45,25 @@ for form in (sphcuda.SPH_MIXED, sphcuda.SPH_F64):
 ctx = sphcuda.SphContext((1.0, 1.0, 0.5), lattice.shape[0], gravity=g, flags=sphcuda.SPH_FLAG_ALL_PAIRS)
 ctx.upload(lattice)
 ctx.step(3)
+flags |= ctx.debug_check()
+ctx.close()
+# the allocation-free grid build (its checks are collected by the next context's check)
+import ctypes, torch
+L = sphcuda.load()
+for box, pos in (((0.5, 0.5, 0.5), clump), ((1.0, 1.0, 0.5), lattice)):
+    n = pos.shape[0]
+    res = [int(np.ceil(np.float32(b) / np.float32(0.0457))) for b in box]
+    xyz = torch.from_numpy(np.ascontiguousarray(pos)).cuda()
+    oc = torch.empty(n, dtype=torch.int32, device="cuda")
+    os_ = torch.empty(res[0] * res[1] * res[2] + 1, dtype=torch.int32, device="cuda")
+    oo = torch.empty(n, dtype=torch.int32, device="cuda")
+    rc = L.sph_grid_build_noalloc(ctypes.c_void_p(xyz.data_ptr()), n, (ctypes.c_float * 3)(*box), 0.0457,
+                                  ctypes.c_void_p(oc.data_ptr()), ctypes.c_void_p(os_.data_ptr()),
+                                  ctypes.c_void_p(oo.data_ptr()), None)
+    torch.cuda.synchronize()
+    assert rc == 0
+    out[f"noalloc/{box}"] = oo.cpu().numpy().tobytes().hex()
+ctx = sphcuda.SphContext((0.4, 0.4, 0.4), 10)
 flags |= ctx.debug_check()
 ctx.close()
 print(json.dumps({"flags": flags, "out": out}))

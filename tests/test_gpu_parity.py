@@ -23,8 +23,10 @@ def c0_scene(sphlib, dims=(20, 20, 20), box=C0_BOX, seed=0):
     return sphlib.dam_break_scene(dims, box, seed)
 
 
-def gpu_run(sphlib, box, pos, vel=None, steps=1, precision=0, gravity=None, flags=2):
+def gpu_run(sphlib, box, pos, vel=None, steps=1, precision=0, gravity=None, flags=2, cell_mult=1):
     ctx = sphlib.SphContext(box, pos.shape[0], precision=precision, flags=flags, gravity=gravity)
+    if cell_mult != 1:
+        ctx.set_cell_multiple(cell_mult)
     ctx.upload(pos, vel)
     ctx.step(steps)
     out = ctx.download(acc=bool(flags & 2))
@@ -94,6 +96,93 @@ def test_grid_bit_exact(sphlib, oracle_mod):
         ctx.close()
 
 
+@pytest.mark.parametrize("prec", ["plain", "mixed"])
+def test_grid_reported_on_half_cells(sphlib, oracle_mod, prec):
+    """On cells of h/2 the step's grid is finer, and sph_get_grid still reports the reference's
+    grid (cells of size h: cell of every particle, counts, (cell, id) order) bit for bit, for a
+    batch of scenes, before and after the particles move."""
+    form = {"plain": sphlib.SPH_PLAIN_F32, "mixed": sphlib.SPH_MIXED}[prec]
+    sc = scenes(sphlib, oracle_mod)
+    names = ["c0_8000_moving", "outside_walls", "dense_clump"]
+    boxes = [sc[k][0] for k in names]
+    parts = [sc[k][1] for k in names]
+    vels = np.concatenate([sc[k][2] for k in names])
+    counts = [p.shape[0] for p in parts]
+    ctx = sphlib.SphContext(boxes, counts, precision=form, gravity=G981)
+    ctx.set_cell_multiple(2)
+    assert ctx.cell_multiple() == 2
+    ctx.upload(np.concatenate(parts), vels, counts)
+    off = np.concatenate([[0], np.cumsum(counts)])
+    for rep in range(2):
+        cur = ctx.download()["pos"]
+        ctx.pass_grid()
+        cell, cnt, order = ctx.grid()
+        cbase = 0
+        for s_, (box, n) in enumerate(zip(boxes, counts)):
+            o = oracle_mod.Oracle(box, oracle_mod.CANON, threads=1)
+            o.add(cur[off[s_]:off[s_ + 1]])
+            o.update_grid()
+            ocell, ocounts, oorder = o.grid()
+            assert np.array_equal(cell[off[s_]:off[s_ + 1]], ocell.astype(np.uint32)), (prec, rep, s_)
+            assert np.array_equal(cnt[cbase:cbase + ocounts.size], ocounts.astype(np.uint32)), (prec, rep, s_)
+            assert np.array_equal(order[off[s_]:off[s_ + 1]], oorder.astype(np.uint32)), (prec, rep, s_)
+            cbase += ocounts.size
+        ctx.pass_density()
+        ctx.pass_forces()
+        ctx.step(3)
+    ctx.close()
+
+
+def test_cell_multiple_errors(sphlib):
+    """Cells of h/2 are for the plain and mixed grid forms and change between steps only."""
+    f64 = sphlib.SphContext(C0_BOX, 100, precision=sphlib.SPH_F64)
+    with pytest.raises(sphlib.SphError) as e:
+        f64.set_cell_multiple(2)
+    assert e.value.code == sphlib.SPH_ERR_UNSUPPORTED
+    f64.close()
+    ap = sphlib.SphContext(C0_BOX, 100, flags=sphlib.SPH_FLAG_ALL_PAIRS)
+    with pytest.raises(sphlib.SphError) as e:
+        ap.set_cell_multiple(2)
+    assert e.value.code == sphlib.SPH_ERR_UNSUPPORTED
+    ap.close()
+    ctx = sphlib.SphContext(C0_BOX, 100)
+    for bad in (0, 3, -1):
+        with pytest.raises(sphlib.SphError) as e:
+            ctx.set_cell_multiple(bad)
+        assert e.value.code == sphlib.SPH_ERR_ARG
+    ctx.set_cell_multiple(2)
+    with pytest.raises(sphlib.SphError) as e:
+        ctx.set_variant(0, 4)  # cells of h/2 run the record variants 7-11 only
+    assert e.value.code == sphlib.SPH_ERR_ARG
+    ctx.upload(c0_scene(sphlib, dims=(4, 5, 5)))
+    ctx.pass_grid()
+    with pytest.raises(sphlib.SphError) as e:
+        ctx.set_cell_multiple(1)
+    assert e.value.code == sphlib.SPH_ERR_STATE
+    ctx.pass_density()
+    ctx.pass_forces()
+    ctx.set_cell_multiple(1)
+    ctx.step(2)
+    assert np.all(np.isfinite(ctx.download()["pos"]))
+    ctx.close()
+
+
+def test_cell_multiple_switch_between_steps(sphlib, oracle_mod):
+    """Switching the cell multiple between steps re-hashes the held particles: a run that switches
+    twice matches the oracle's run of the same steps within the one-step band per step."""
+    box, pos, vel, g = scenes(sphlib, oracle_mod)["c0_8000_moving"]
+    ctx = sphlib.SphContext(box, pos.shape[0], gravity=g, flags=sphlib.SPH_FLAG_RECORD_ACC)
+    ctx.upload(pos, vel)
+    for m in (2, 1, 2):
+        cur = ctx.download()
+        ctx.set_cell_multiple(m)
+        ctx.step(1)
+        got = ctx.download(acc=True)
+        ref = oracle_run(oracle_mod, box, cur["pos"], cur["vel"], gravity=g)
+        assert_within(rel_errors(got, ref), f"switch to cells h/{m}")
+    ctx.close()
+
+
 def test_grid_cell_faces(sphlib, oracle_mod):
     """Coordinates on and one ulp around every cell face hash exactly as the double formula."""
     box = (0.4, 0.4, 0.4)
@@ -117,13 +206,67 @@ def test_grid_cell_faces(sphlib, oracle_mod):
     ctx.close()
 
 
+def crowded_scene(seed=4):
+    """Cells far above rest occupancy: one cell of 2,500 particles (sorted in shared memory), one of
+    20,000 (above the 4,096 that are sorted; those are counted), 40 cells of 100-160 (around the
+    128 that are counted directly), and a sparse lattice around them."""
+    rng = np.random.default_rng(seed)
+    box = (0.6, 0.6, 0.6)
+    h = float(H32)
+    parts = []
+    for cidx, n in (((2, 3, 4), 2500), ((8, 8, 8), 20000)):
+        lo = np.array(cidx) * h - 0.3
+        parts.append(lo + (0.05 + 0.9 * rng.random((n, 3))) * h)
+    for k in range(40):
+        cidx = rng.integers(0, 13, 3)
+        lo = cidx * h - 0.3
+        parts.append(lo + (0.05 + 0.9 * rng.random((int(rng.integers(100, 161)), 3))) * h)
+    g = np.stack(np.meshgrid(*[np.arange(6) * 0.09 - 0.25] * 3, indexing="ij"), -1).reshape(-1, 3)
+    parts.append(g)
+    pos = np.concatenate(parts).astype(np.float32)
+    return box, pos[rng.permutation(pos.shape[0])]
+
+
+@pytest.mark.parametrize("prec", ["plain", "mixed", "f64"])
+def test_grid_crowded_cells_bit_exact(sphlib, oracle_mod, prec):
+    """The canonical (cell, id) order in cells of thousands of particles (sorted slot ids and a
+    lower-bound rank) and of tens of thousands (counted) equals the oracle's grid bit for bit,
+    in every precision form, before and after the particles move."""
+    box, pos = crowded_scene()
+    form = {"plain": sphlib.SPH_PLAIN_F32, "mixed": sphlib.SPH_MIXED, "f64": sphlib.SPH_F64}[prec]
+    # a short time step keeps the crowded particles (pressures far above any physical state)
+    # near their cells for the second grid pass, which starts from the force pass's hashes
+    ctx = sphlib.SphContext(box, pos.shape[0], precision=form, params=sphlib.default_params(dt=1e-5, gravity=G981))
+    ctx.upload(pos)
+    # FP64 positions are compared from the upload only: their float copies could round across a face
+    for rep in range(1 if prec == "f64" else 2):
+        cur = ctx.download()["pos"] if rep else pos
+        assert np.all(np.isfinite(cur))
+        ctx.pass_grid()
+        cell, counts, order = ctx.grid()
+        assert counts.max() >= 20000 and np.sum(counts > 128) >= 15 and np.sum((counts > 32) & (counts <= 128)) >= 5
+        o = oracle_mod.Oracle(box, oracle_mod.CANON, threads=1)
+        o.add(cur)
+        o.update_grid()
+        ocell, ocounts, oorder = o.grid()
+        assert np.array_equal(cell, ocell.astype(np.uint32)), (prec, rep)
+        assert np.array_equal(counts, ocounts.astype(np.uint32)), (prec, rep)
+        assert np.array_equal(order, oorder.astype(np.uint32)), (prec, rep)
+        ctx.pass_density()
+        ctx.pass_forces()
+    ctx.close()
+
+
 # ------------------------------------------------------------------------- one step
+@pytest.mark.parametrize("cell_mult", [1, 2])
 @pytest.mark.parametrize("name", ["ref_default_0.4", "c0_8000", "c0_8000_moving", "outside_walls", "dense_clump"])
-def test_one_step_plain_vs_oracle(sphlib, oracle_mod, name):
+def test_one_step_plain_vs_oracle(sphlib, oracle_mod, name, cell_mult):
+    """One plain FP32 step per particle against the oracle, on the reference's cells of size h
+    and on cells of h/2 (the same method, candidates summed in another order)."""
     box, pos, vel, g = scenes(sphlib, oracle_mod)[name]
-    got = gpu_run(sphlib, box, pos, vel, gravity=g)
+    got = gpu_run(sphlib, box, pos, vel, gravity=g, cell_mult=cell_mult)
     ref = oracle_run(oracle_mod, box, pos, vel, gravity=g)
-    assert_within(rel_errors(got, ref), name)
+    assert_within(rel_errors(got, ref), f"{name}/cells h/{cell_mult}")
 
 
 @pytest.mark.parametrize("name", ["ref_default_0.4", "c0_8000_moving", "outside_walls"])
@@ -168,29 +311,47 @@ def test_golden_cases_on_gpu(sphlib, case):
 
 
 # ------------------------------------------------------------------------- long runs
-def test_bands_vs_f64_c0(sphlib):
-    """8,000-particle dam break, 200 steps: per-step mean/max density, kinetic energy and mass
-    of the plain FP32 run stay within bands of the FP64 GPU run (the flow is chaotic: single
-    particles decorrelate after ~30 steps)."""
-    pos = c0_scene(sphlib)
-    ctx = {p: sphlib.SphContext(C0_BOX, pos.shape[0], precision=p, gravity=G981) for p in (0, 1)}
-    for c in ctx.values():
-        c.upload(pos)
-    worst = {"mean": 0.0, "max": 0.0, "ke": 0.0}
-    for step in range(200):
-        for c in ctx.values():
-            c.step(1)
-        if step % 10 == 9:
-            s32, s64 = ctx[0].stats(), ctx[1].stats()
-            assert s32["count"] == s64["count"] == pos.shape[0]
-            assert s32["mass"] == s64["mass"]
-            worst["mean"] = max(worst["mean"], abs(s32["rho_mean"] - s64["rho_mean"]) / s64["rho_mean"])
-            worst["max"] = max(worst["max"], abs(s32["rho_max"] - s64["rho_max"]) / s64["rho_max"])
-            if s64["kinetic"] > 1e-3:
-                worst["ke"] = max(worst["ke"], abs(s32["kinetic"] - s64["kinetic"]) / s64["kinetic"])
-    assert worst["mean"] < 2e-2 and worst["max"] < 2e-1 and worst["ke"] < 3e-1, worst
-    d = ctx[0].download()
+def dam8k_aggregates(sphlib, prec, pos, steps=200, every=10):
+    c = sphlib.SphContext(C0_BOX, pos.shape[0], precision=prec, gravity=G981)
+    c.upload(pos)
+    out = []
+    for s in range(steps):
+        c.step(1)
+        if s % every == every - 1:
+            st = c.stats()
+            out.append((st["rho_mean"], st["rho_max"], st["kinetic"], st["mass"]))
+    d = c.download()
     assert np.all(np.isfinite(d["pos"])) and np.all(np.isfinite(d["rho"]))
+    c.close()
+    return np.array(out)
+
+
+@pytest.fixture(scope="module")
+def dam8k_fp64(sphlib):
+    """The 8,000-particle dam break's FP64 run and the envelope of its chaotic spread: three FP64
+    runs from the same lattice with every coordinate moved by one float ulp (random signs)."""
+    from test_config_scale import spread_envelope, ulp_perturb
+
+    pos = c0_scene(sphlib)
+    ref = dam8k_aggregates(sphlib, sphlib.SPH_F64, pos)
+    pert = [dam8k_aggregates(sphlib, sphlib.SPH_F64, ulp_perturb(pos, k)) for k in (1, 2, 3)]
+    return pos, ref, spread_envelope(ref, pert)
+
+
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_bands_vs_f64_c0(sphlib, dam8k_fp64, form):
+    """8,000-particle dam break, 200 steps: every 10 steps the form's mean and max density and
+    kinetic energy stay within 3 times the FP64 runs' spread envelope plus the form's floor
+    (1e-5 plain, 3e-3 mixed, relative); mass is exact."""
+    from test_config_scale import FLOOR, band_ratio
+
+    pos, ref, env = dam8k_fp64
+    prec = {"plain": sphlib.SPH_PLAIN_F32, "mixed": sphlib.SPH_MIXED}[form]
+    got = dam8k_aggregates(sphlib, prec, pos)
+    assert np.array_equal(got[:, 3], ref[:, 3])
+    worst = band_ratio(got, ref, env, FLOOR[form])
+    print(f"dam8k {form}: worst deviation / band {worst:.3f}")
+    assert worst <= 1.0, worst
 
 
 # ------------------------------------------------------------------------- batches
@@ -475,12 +636,36 @@ def test_online_tuning_keeps_the_bits(sphlib):
     for r in runs[1:]:
         for k in runs[0]:
             assert np.array_equal(runs[0][k], r[k]), k
-    m = sphlib.SphContext(C0_BOX, 10, precision=sphlib.SPH_MIXED)
-    with pytest.raises(sphlib.SphError) as e:
-        m.set_online_tuning(10)
-    assert e.value.code == sphlib.SPH_ERR_STATE
     with pytest.raises(sphlib.SphError) as e:
         sphlib.SphContext(C0_BOX, 10).set_online_tuning(3)
+    assert e.value.code == sphlib.SPH_ERR_ARG
+    # the mixed form: its four launch forms give the same bits, so online tuning keeps them too
+    runs = []
+    for mode in ("fixed", "online_step", "online_passes"):
+        m = sphlib.SphContext(C0_BOX, pos.shape[0], precision=sphlib.SPH_MIXED, gravity=G981,
+                              flags=sphlib.SPH_FLAG_RECORD_ACC)
+        m.upload(pos)
+        m.set_variant(0, 0)
+        if mode != "fixed":
+            m.set_online_tuning(4)
+        if mode == "online_passes":
+            for _ in range(23):
+                m.pass_grid()
+                m.pass_density()
+                m.pass_forces()
+        else:
+            m.step(11)
+            m.step(12)
+        if mode != "fixed":
+            assert m.variant()[1] in (0, 1, 2, 3)
+        runs.append(m.download(acc=True))
+        m.close()
+    for r in runs[1:]:
+        for k in runs[0]:
+            assert np.array_equal(runs[0][k], r[k]), ("mixed", k)
+    m = sphlib.SphContext(C0_BOX, 10, precision=sphlib.SPH_MIXED)
+    with pytest.raises(sphlib.SphError) as e:
+        m.set_variant(0, 4)  # the mixed form has force variants 0-3 only
     assert e.value.code == sphlib.SPH_ERR_ARG
     m.close()
 
@@ -825,26 +1010,99 @@ def test_variants_bit_identical(sphlib, oracle_mod):
                     assert np.array_equal(out[k], base[k]), (dv, fv, k)
 
 
+@pytest.mark.parametrize("cell_mult", [1, 2])
+def test_mixed_variants_bit_identical(sphlib, oracle_mod, cell_mult):
+    """The mixed form's four force launch forms compute the same bits (also on the dense clump,
+    whose rows run past the recorded mask words), on cells of h and of h/2."""
+    for box, pos, vel, g in [scenes(sphlib, oracle_mod)["c0_8000_moving"],
+                             scenes(sphlib, oracle_mod)["dense_clump"]]:
+        base = None
+        for fv in range(4):
+            ctx = sphlib.SphContext(box, pos.shape[0], precision=sphlib.SPH_MIXED, gravity=g, flags=2)
+            ctx.set_cell_multiple(cell_mult)
+            ctx.set_variant(0, fv)
+            ctx.upload(pos, vel)
+            ctx.step(6)
+            out = ctx.download(acc=True)
+            ctx.close()
+            if base is None:
+                base = out
+            for k in out:
+                assert np.array_equal(out[k], base[k]), (fv, k)
+
+
+def test_half_cell_variants_bit_identical(sphlib, oracle_mod):
+    """On cells of h/2 the record variants 7 to 11 compute the same bits."""
+    for box, pos, vel, g in [scenes(sphlib, oracle_mod)["c0_8000_moving"],
+                             scenes(sphlib, oracle_mod)["dense_clump"]]:
+        base = None
+        for fv in (7, 8, 9, 10, 11):
+            ctx = sphlib.SphContext(box, pos.shape[0], gravity=g, flags=2)
+            ctx.set_cell_multiple(2)
+            ctx.set_variant(0, fv)
+            ctx.upload(pos, vel)
+            ctx.step(6)
+            out = ctx.download(acc=True)
+            ctx.close()
+            if base is None:
+                base = out
+            for k in out:
+                assert np.array_equal(out[k], base[k]), (fv, k)
+
+
+def test_mixed_half_cells_vs_f64(sphlib, oracle_mod):
+    """The mixed form on cells of h/2, one step against the FP64 run: density within 1e-3."""
+    for name in ("ref_default_0.4", "c0_8000_moving", "outside_walls"):
+        box, pos, vel, g = scenes(sphlib, oracle_mod)[name]
+        m = sphlib.SphContext(box, pos.shape[0], precision=sphlib.SPH_MIXED, flags=2, gravity=g)
+        m.set_cell_multiple(2)
+        m.upload(pos, vel)
+        m.step(1)
+        got = m.download(acc=True)
+        m.close()
+        ref = gpu_run(sphlib, box, pos, vel, steps=1, precision=sphlib.SPH_F64, gravity=g)
+        assert np.max(np.abs(got["rho"] - ref["rho"]) / ref["rho"]) < 1e-3, name
+
+
 def test_autotune_is_one_plain_step(sphlib, tmp_path, monkeypatch):
     monkeypatch.setenv("SPH_TUNE_CACHE", str(tmp_path / "tune.txt"))
     pos = c0_scene(sphlib)
     a = sphlib.SphContext(C0_BOX, pos.shape[0], gravity=G981, flags=2)
     a.upload(pos)
     dv, fv = a.autotune(reps=2)
-    assert dv in (0, 1, 2, 4) and fv in (0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11)
+    cm = a.cell_multiple()
+    assert dv in (0, 1, 2, 4) and fv in (0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11) and cm in (1, 2)
     a.step(3)
-    b = gpu_run(sphlib, C0_BOX, pos, steps=4, gravity=G981)
+    # the same four steps with the chosen cell multiple and variants, set by hand
+    ref = sphlib.SphContext(C0_BOX, pos.shape[0], gravity=G981, flags=2)
+    ref.set_cell_multiple(cm)
+    ref.set_variant(dv, fv)
+    ref.upload(pos)
+    ref.step(4)
+    b = ref.download(acc=True)
+    ref.close()
     got = a.download(acc=True)
     for k in got:
         assert np.array_equal(got[k], b[k]), k
     line = (tmp_path / "tune.txt").read_text().strip().splitlines()[-1]
-    assert line.endswith(f" {dv} {fv}") and "|b12" in line  # 8000 particles -> bucket 12
-    # a new context of the same bucket picks the cached variants at upload
+    assert line.endswith(f" {dv} {fv} {cm}") and "|b12" in line  # 8000 particles -> bucket 12
+    # a new context of the same bucket picks the cached choice at upload
     c = sphlib.SphContext(C0_BOX, pos.shape[0], gravity=G981)
     c.upload(pos)
-    assert c.variant() == (dv, fv)
+    assert c.variant() == (dv, fv) and c.cell_multiple() == cm
     a.close()
     c.close()
+    # a cached line for cells of h/2 is applied before the upload's hash
+    (tmp_path / "tune.txt").write_text(line.rsplit(" ", 3)[0] + " 0 9 2\n")
+    d = sphlib.SphContext(C0_BOX, pos.shape[0], gravity=G981, flags=2)
+    d.upload(pos)
+    assert d.variant() == (0, 9) and d.cell_multiple() == 2
+    d.step(2)
+    e2 = gpu_run(sphlib, C0_BOX, pos, steps=2, gravity=G981, cell_mult=2)
+    dd = d.download(acc=True)
+    for k in dd:
+        assert np.array_equal(dd[k], e2[k]), k
+    d.close()
 
 
 def test_upload_step_download_equals_resident(sphlib):
@@ -893,26 +1151,6 @@ def test_mixed_one_step_vs_f64(sphlib, oracle_mod):
             (2e-3 * scale * 1e-4)[:, None]
         pos_err = np.max(np.abs(x64 - ref["pos"]) / bound)
         assert rho_err < 1e-3 and acc_err < 2e-3 and pos_err <= 1.0, (name, rho_err, acc_err, pos_err)
-
-
-def test_mixed_bands_vs_f64_c0(sphlib):
-    """200 steps of the 8,000-particle dam break: mixed aggregates within the plain form's bands."""
-    pos = c0_scene(sphlib)
-    ctx = {p: sphlib.SphContext(C0_BOX, pos.shape[0], precision=p, gravity=G981) for p in (2, 1)}
-    for c in ctx.values():
-        c.upload(pos)
-    worst = {"mean": 0.0, "max": 0.0, "ke": 0.0}
-    for step in range(200):
-        for c in ctx.values():
-            c.step(1)
-        if step % 10 == 9:
-            s, s64 = ctx[2].stats(), ctx[1].stats()
-            assert s["mass"] == s64["mass"]
-            worst["mean"] = max(worst["mean"], abs(s["rho_mean"] - s64["rho_mean"]) / s64["rho_mean"])
-            worst["max"] = max(worst["max"], abs(s["rho_max"] - s64["rho_max"]) / s64["rho_max"])
-            if s64["kinetic"] > 1e-3:
-                worst["ke"] = max(worst["ke"], abs(s["kinetic"] - s64["kinetic"]) / s64["kinetic"])
-    assert worst["mean"] < 2e-2 and worst["max"] < 2e-1 and worst["ke"] < 3e-1, worst
 
 
 def test_mixed_ten_steps_vs_f64(sphlib):

@@ -67,6 +67,16 @@ def test_lattice_bit_exact(sphlib, dims, box, seed):
     assert np.all(got.min(axis=0) <= lo + 0.0101 * SPACING)
 
 
+@pytest.mark.parametrize("dims,box,seed", [((20, 20, 20), (1.0, 1.0, 0.5), 0), ((7, 3, 5), (0.5, 0.3, 0.4), 12345),
+                                            ((100, 100, 100), (5.0, 5.0, 2.5), 1)])
+def test_oracle_lattice_equals_library_lattice(sphlib, dims, box, seed):
+    """The oracle's vectorised restatement (the reference arm's input, built without the
+    product library) gives the library generator's coordinates bit for bit, up to the 1M scene."""
+    from oracle import scenes
+
+    assert np.array_equal(scenes.dam_break(dims, box, seed), sphlib.dam_break_scene(dims, box, seed))
+
+
 def test_batch_plan(sphlib):
     dims, boxes = sphlib.batch_plan(256, seed=3)
     rng = SplitMix64(3)
