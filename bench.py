@@ -393,9 +393,7 @@ def run_reference(args):
 
         boxes, pos, counts, caps, obs, emit, desc = build_config(sphcuda, args.config)
         if len(boxes) != 1:
-            print(json.dumps({"impl": "reference", "unavailable": f"config {args.config}: the oracle runs one "
-                              "scene"}))
-            return 0
+            return run_reference_batch(args, O, boxes, pos, counts, desc, threads)
         box, obstacles = boxes[0], (obs[0] if obs else None)
     o = O.Oracle(box, O.REF, threads=threads, gravity=GRAVITY, obstacles=obstacles)
     if pos.shape[0]:
@@ -452,6 +450,37 @@ def run_reference(args):
     return 0
 
 
+def run_reference_batch(args, O, boxes, pos, counts, desc, threads):
+    """The reference's CPU step on a batch of scenes: one oracle per scene, every scene
+    stepped once per step (the reference simulates one scene at a time)."""
+    off = np.concatenate([[0], np.cumsum(counts)])
+    sims = []
+    for s_, box in enumerate(boxes):
+        o = O.Oracle(box, O.REF, threads=threads, gravity=GRAVITY)
+        o.add(pos[off[s_]:off[s_ + 1]])
+        sims.append(o)
+    for _ in range(args.warmup):
+        for o in sims:
+            o.step(1)
+    t0 = time.perf_counter()
+    done = 0
+    while done < args.steps:
+        for o in sims:
+            o.step(1)
+        done += 1
+        if time.perf_counter() - t0 > args.ref_budget:
+            break
+    el = time.perf_counter() - t0
+    value = int(off[-1]) * done / el
+    print(json.dumps({"impl": "reference", "config": {"workload": desc}, "value": value, "unit": UNIT, "steps": done,
+                      "warmup": args.warmup, "cores": threads, "ms_per_step": 1000 * el / done,
+                      "sample": f"{done} whole steps of all {len(boxes)} scenes after {args.warmup} warm-up steps, "
+                                f"one oracle per scene, density/force passes on {threads} threads"}), flush=True)
+    for o in sims:
+        o.close()
+    return 0
+
+
 def build_config(sphcuda, name, seed=0):
     """Scenes of the other benchmark configurations: (boxes, positions, counts, capacities,
     obstacles, emitter or None, description)."""
@@ -491,6 +520,32 @@ def build_config(sphcuda, name, seed=0):
             "box scaled x4.57 so the lattice fits; it fills the upstream half), 8 seeded box obstacles of "
             "0.23-0.91 m in the downstream half")
     raise ValueError(name)
+
+
+def config_fp64_error(sphcuda, ctx, form, boxes, obstacles, sample=1_000_000):
+    """Max relative density error and acceleration error (of the largest FP64 acceleration) of
+    one step from the run's final state against an FP64 context of the same scenes, over a seeded
+    sample of at most `sample` particles."""
+    counts = list(ctx.counts())
+    st = ctx.download()
+    out = {}
+    for name, prec in (("form", form), ("f64", sphcuda.SPH_F64)):
+        c = sphcuda.SphContext(boxes, counts, precision=prec, gravity=GRAVITY, obstacles=obstacles,
+                               flags=sphcuda.SPH_FLAG_RECORD_ACC)
+        if prec != sphcuda.SPH_F64:
+            c.set_cell_multiple(ctx.cell_multiple())
+        c.upload(st["pos"], st["vel"], counts)
+        c.step(1)
+        d = c.download(acc=True)
+        out[name] = {"rho": d["rho"].astype(np.float64), "acc": d["acc"].astype(np.float64)}
+        c.close()
+    n = out["f64"]["rho"].shape[0]
+    sub = np.random.default_rng(5).choice(n, min(n, sample), replace=False)
+    a, b = out["form"], out["f64"]
+    amax = float(np.max(np.linalg.norm(b["acc"][sub], axis=1)))
+    return {"after": "one step from the run's final state", "particles_compared": int(sub.size),
+            "rho_max_rel": float(np.max(np.abs(a["rho"][sub] - b["rho"][sub]) / b["rho"][sub])),
+            "acc_max_err_over_max_acc": float(np.max(np.linalg.norm(a["acc"][sub] - b["acc"][sub], axis=1)) / amax)}
 
 
 def run_config(args):
@@ -547,11 +602,13 @@ def run_config(args):
     work = advance(args.steps, ms)
     st = ctx.stats(0)
     finite = bool(np.isfinite(st["rho_mean"]))
+    check = config_fp64_error(sphcuda, ctx, form, boxes, obstacles) if args.fp64_check else None
     line = {"metric": METRIC, "value": work / (sum(ms) / 1000.0), "unit": UNIT, "config": {"workload": desc,
             "form": args.form, "particles_final": ctx.n, "scenes": len(boxes)}, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": sum(ms) / args.steps,
             "launch_variant": list(ctx.variant()), "cell_multiple": ctx.cell_multiple(),
-            "finite": finite, "rho_mean_scene0": st["rho_mean"], "l2": "not flushed (replayed steps)"}
+            "finite": finite, "rho_mean_scene0": st["rho_mean"], "l2": "not flushed (replayed steps)",
+            "fp64_check": check}
     ctx.close()
     print(json.dumps(line), flush=True)
     return 0
@@ -587,6 +644,8 @@ def main():
                     help="steps of the run over which the timed steps are spread (default: the configuration's "
                          "500; e.g. a few steps to profile a state given by --init-state)")
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-scene batch leg")
+    ap.add_argument("--fp64-check", action="store_true",
+                    help="other configurations: one step from the final state against FP64 (density, acceleration)")
     ap.add_argument("--cell-multiple", type=int, default=0,
                     help="pin the step grid's cell multiple (1: cells of h, 2: cells of h/2) instead of autotuning it")
     args = ap.parse_args()

@@ -37,6 +37,7 @@ struct SceneHost {
 enum State { EMPTY = 0, HASHED = 1, SORTED = 2, DENSE = 3 };
 
 constexpr int kOnlineN = 4;  // force variants tried by online tuning (one trial step each)
+constexpr int kOnlineMax = kOnlineN + 1;  // ... and one trial on the other cell multiple
 
 thread_local std::string g_create_error;
 
@@ -67,6 +68,7 @@ struct sph_ctx {
     std::vector<uint32_t> scene_off_host;
     Tune tune;
     bool tune_pinned = false;  // variants set explicitly: the cache does not override them
+    bool cell_pinned = false;  // cell multiple set explicitly: the autotuner keeps it
     // front-end handoff (allocated by the first handoff or export)
     cudaStream_t ho_stream = nullptr;
     cudaEvent_t ho_ready = nullptr, ho_done = nullptr, ho_export = nullptr;
@@ -76,7 +78,10 @@ struct sph_ctx {
     int online_period = 0;     // steps between trials; 0 = off
     uint64_t steps_run = 0;    // whole steps run by this context
     int trial = -1;            // candidate being timed in this step, -1 = none
-    float trial_ms[kOnlineN] = {};  // one per online candidate
+    int n_trials = 0;          // candidates of the current trial period
+    float trial_ms[kOnlineMax] = {};  // one per online candidate
+    int trial_m[kOnlineMax] = {}, trial_v[kOnlineMax] = {};  // its cell multiple and force variant
+    int last_best_v[3] = {0, 10, 10};  // per cell multiple, the force variant its last trials kept
     cudaEvent_t on_ev[2] = {nullptr, nullptr};
     int graph_forces = -1;     // force variant captured in the graph
     std::vector<unsigned char *> canaries;  // checked builds: the guard region after each array
@@ -253,7 +258,7 @@ size_t pool_layout(sph_ctx *c, std::vector<PoolItem> &items)
         {(void **) &b.bsum, 4 * nb}, {(void **) &b.big, 4 * big_words(N)},
         {(void **) &b.scenes, sizeof(SceneDev) * c->sc.size()},
         {(void **) &b.obstacles, sizeof(ObstacleDev) * (nobs ? nobs : 1)},
-        {(void **) &b.scene_off, 4 * (c->sc.size() + 1)}, {(void **) &b.err, 16}, {(void **) &b.tiles, 16},
+        {(void **) &b.scene_off, 4 * (c->sc.size() + 1)}, {(void **) &b.err, 16},
         {(void **) &b.st_xyz, 12 * N}, {(void **) &b.st_vel, 12 * N},
         {(void **) &b.st_rho, rs == 4 ? 4 * N : 0}, {(void **) &b.st_p, rs == 4 ? 4 * N : 0},
         {(void **) &b.st_acc, rs == 4 && rec ? 12 * N : 0},
@@ -566,16 +571,41 @@ int online_candidate(const sph_ctx *c, int k) { return is_mixed(c) ? kOnlineCand
 bool online_active(const sph_ctx *c)
 {
     if (c->online_period <= 0) return false;
-    return is_mixed(c) || (c->tune.forces_mode >= 3 && c->tune.forces_mode <= 12);
+    return is_mixed(c) || (c->tune.forces_mode >= 3 && c->tune.forces_mode <= 11);
 }
 
 // before a step: start a due trial and set this step's candidate
+int set_cell_mult(sph_ctx *c, int m);
+bool cell_mult_allowed(const sph_ctx *c, int m, uint64_t ctot_ref);
+
+// A trial period times the form's four variants on the current cell multiple and, unless the
+// multiple was set by the caller, the other multiple once (with the variant its last trials
+// kept): the column's state decides which grid is faster, and it changes over a run.
 int online_begin_step(sph_ctx *c)
 {
     if (!online_active(c)) return SPH_OK;
-    if (c->trial < 0 && c->steps_run % (uint64_t) c->online_period == 0) c->trial = 0;
+    if (c->trial < 0 && c->steps_run % (uint64_t) c->online_period == 0) {
+        c->trial = 0;
+        c->n_trials = 0;
+        const int m = c->tune.cell_mult;
+        for (int k = 0; k < kOnlineN; k++, c->n_trials++) {
+            c->trial_m[c->n_trials] = m;
+            c->trial_v[c->n_trials] = online_candidate(c, k);
+        }
+        const int other = m == 1 ? 2 : 1;
+        if (!c->cell_pinned && cell_mult_allowed(c, other, c->ctot_ref)) {
+            c->trial_m[c->n_trials] = other;
+            c->trial_v[c->n_trials] = is_mixed(c) ? std::min(c->last_best_v[other], kMixedVariants - 1)
+                                                  : std::max(7, c->last_best_v[other]);
+            c->n_trials++;
+        }
+    }
     if (c->trial < 0) return SPH_OK;
-    c->tune.forces_mode = online_candidate(c, c->trial);
+    if (c->trial_m[c->trial] != c->tune.cell_mult) {  // re-hash into the other grid (not timed)
+        const int rc = set_cell_mult(c, c->trial_m[c->trial]);
+        if (rc) return rc;
+    }
+    c->tune.forces_mode = c->trial_v[c->trial];
     CK(c, cudaEventRecord(c->on_ev[0], c->stream));
     return SPH_OK;
 }
@@ -588,17 +618,28 @@ int online_end_step(sph_ctx *c)
     CK(c, cudaEventRecord(c->on_ev[1], c->stream));
     CK(c, cudaEventSynchronize(c->on_ev[1]));
     c->trial_ms[c->trial] = elapsed(c->on_ev[0], c->on_ev[1]);
-    if (++c->trial < kOnlineN) return SPH_OK;
+    if (++c->trial < c->n_trials) return SPH_OK;
     int best = 0;
-    for (int k = 1; k < kOnlineN; k++)
+    for (int k = 1; k < c->n_trials; k++)
         if (c->trial_ms[k] < c->trial_ms[best]) best = k;
-    c->tune.forces_mode = online_candidate(c, best);
+    // the best variant of each multiple tried, for that multiple's next trial
+    for (int m = 1; m <= 2; m++) {
+        int bm = -1;
+        for (int k = 0; k < c->n_trials; k++)
+            if (c->trial_m[k] == m && (bm < 0 || c->trial_ms[k] < c->trial_ms[bm])) bm = k;
+        if (bm >= 0) c->last_best_v[m] = c->trial_v[bm];
+    }
     c->trial = -1;
+    if (c->trial_m[best] != c->tune.cell_mult) {
+        const int rc = set_cell_mult(c, c->trial_m[best]);
+        if (rc) return rc;
+    }
+    c->tune.forces_mode = c->trial_v[best];
     return SPH_OK;
 }
 
 bool valid_density(int v) { return v == 0 || v == 1 || v == 2 || v == 4; }
-bool valid_forces(int v) { return v >= 0 && v <= 12; }
+bool valid_forces(int v) { return v >= 0 && v <= 11; }
 // the mixed form has its own force variants and one density pass (density variant 0); cells of
 // h/2 run the plain form's record variants 7 to 11
 bool valid_variant(const sph_ctx *c, int dv, int fv, int cell_mult)
@@ -1123,8 +1164,11 @@ int sph_autotune(sph_ctx *c, int32_t reps)
     struct Cfg { int d, f; };
     float best = 1e30f;
     int bm = c->tune.cell_mult, bd = c->tune.density_p, bf = c->tune.forces_mode;
-    std::vector<int> mults = {1};
-    if (cell_mult_allowed(c, 2, c->ctot_ref)) mults.push_back(2);
+    // a cell multiple set with sph_set_cell_multiple stays; else both are tried
+    std::vector<int> mults = {c->tune.cell_mult};
+    if (!c->cell_pinned)
+        for (int m = 1; m <= kMaxCellMult; m++)
+            if (m != c->tune.cell_mult && cell_mult_allowed(c, m, c->ctot_ref)) mults.push_back(m);
     for (size_t mi = 0; mi < mults.size(); mi++) {
         const int m = mults[mi];
         if (mi > 0) {
@@ -1149,7 +1193,7 @@ int sph_autotune(sph_ctx *c, int32_t reps)
         } else {
             for (int d : {0, 1, 2, 4})
                 for (int f = 0; f <= 2; f++) cfgs.push_back({d, f});
-            for (int f = 3; f <= 12; f++) cfgs.push_back({0, f});
+            for (int f = 3; f <= 11; f++) cfgs.push_back({0, f});
         }
         for (const Cfg &g : cfgs) {
             c->tune.density_p = g.d;
@@ -1203,7 +1247,7 @@ int sph_set_cell_multiple(sph_ctx *c, int32_t m)
         return fail(c, SPH_ERR_STATE, "the cell multiple changes between steps (not between passes)");
     CK(c, cudaSetDevice(c->device));
     const int rc = set_cell_mult(c, m);
-    if (!rc) c->tune_pinned = true;
+    if (!rc) c->tune_pinned = c->cell_pinned = true;
     return rc;
 }
 

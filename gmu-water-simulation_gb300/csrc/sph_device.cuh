@@ -129,24 +129,6 @@ __device__ __forceinline__ uint32_t hash_cell(const SceneDev &sc, R x, R y, R z,
            (uint32_t) cz * (uint32_t) sc.res[0] * (uint32_t) sc.res[1];
 }
 
-// Row r of the stencil around cell (cx, cy, cz): its candidate range [jb, je), or false if the
-// row lies outside the grid.
-template <int RAD>
-__device__ __forceinline__ bool stencil_row(const SceneDev &sc, const uint32_t *__restrict__ start, int cx, int cy,
-                                            int cz, int r, uint32_t &jb, uint32_t &je)
-{
-    const int D = 2 * RAD + 1;
-    const int dz = r / D - RAD, dy = r % D - RAD;
-    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
-    const int z = cz + dz, y = cy + dy;
-    if (z < 0 || z >= Z || y < 0 || y >= Y) return false;
-    const int xl = cx - RAD > 0 ? cx - RAD : 0, xh = cx + RAD < X ? cx + RAD : X - 1;
-    const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
-    jb = __ldg(start + row + xl);
-    je = __ldg(start + row + xh + 1);
-    return true;
-}
-
 __device__ __forceinline__ SceneDev load_scene(const SceneDev *scenes, uint32_t s)
 {
     SceneDev sc;

@@ -63,7 +63,6 @@ struct DevBufs {
     ObstacleDev *obstacles;
     uint32_t *scene_off;   // first output index of every scene (id-order downloads)
     int32_t *err;          // device error flag
-    uint32_t *tiles;       // tile counters of the persistent launches (density, forces), zeroed before each
     // staging for host transfers (ingest / egress)
     float *st_xyz, *st_vel, *st_rho, *st_p, *st_acc;
     double *st_xyz64, *st_vel64, *st_rho64, *st_p64, *st_acc64;
@@ -126,8 +125,7 @@ struct MixConsts {
 //               neighbour per iteration without/with a 64-register cap, 5/6 two per
 //               iteration with/without it, 7 as 6 with each neighbour's terms read from one
 //               packed force record (two 16-byte loads from one 32-byte record), 8 and 9 as
-//               7 at 48 and 40 registers, 10 and 11 as 9 and 8 in blocks of 128 threads; 12 = 10 with
-//               both neighbour passes as persistent launches over dynamically fetched tiles
+//               7 at 48 and 40 registers, 10 and 11 as 9 and 8 in blocks of 128 threads
 //   cell_mult : the step grid's cells are h / cell_mult wide (1 or 2); the neighbour passes walk
 //               (2 cell_mult + 1)^2 rows of 2 cell_mult + 1 cells (only the mask-driven record
 //               variants, 7 to 11 and the mixed form's, run on cells of h/2)

@@ -408,14 +408,15 @@ __global__ void __launch_bounds__(BLOCK) k_forces_list(
 // WORDS chunks are not recorded: the force pass tests them itself. RAD = 1 is the reference's
 // 27 cells of size h; RAD = 2 walks 125 cells of size h/2 (42% less volume than 27 h^3).
 
-template <class R, bool REC, int RAD>
-__device__ __forceinline__ void density_mask_one(uint32_t i, const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
-                                                 const uint32_t *__restrict__ start,
-                                                 const SceneDev *__restrict__ scenes, uint32_t n, const Consts<R> &c,
-                                                 uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ vel,
-                                                 Vec4<R> *__restrict__ frec)
+template <class R, bool REC, int RAD = 1>
+__global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
+                                                      const uint32_t *__restrict__ start,
+                                                      const SceneDev *__restrict__ scenes, uint32_t n, Consts<R> c,
+                                                      uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ vel,
+                                                      Vec4<R> *__restrict__ frec)
 {
     using St = Stencil<RAD>;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const Vec4<R> pi = ld4(pos + i);
     const SceneDev sc = load_scene(scenes, wbits(pi.w));
@@ -423,26 +424,34 @@ __device__ __forceinline__ void density_mask_one(uint32_t i, const Vec4<R> *__re
     hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
     const R h2 = c.h2;
     R acc = 0;
+    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
+    const int xl = cx - RAD > 0 ? cx - RAD : 0, xh = cx + RAD < X ? cx + RAD : X - 1;
 #pragma unroll 1
-    for (int r = 0; r < St::ROWS; r++) {
-        uint32_t jb, je;
-        if (!stencil_row<RAD>(sc, start, cx, cy, cz, r, jb, je)) continue;
-        if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
-        int w = 0;
-        for (uint32_t cb = jb; cb < je; cb += 32, w++) {
-            // bit k of the chunk's word = candidate cb + k; bits enter at the top and
-            // move down one place per candidate
-            const uint32_t ce = min(je, cb + 32u);
-            uint32_t m = 0;
+    for (int dz = -RAD; dz <= RAD; dz++) {
+#pragma unroll 1
+        for (int dy = -RAD; dy <= RAD; dy++) {
+            const int r = (dz + RAD) * (2 * RAD + 1) + (dy + RAD);
+            const int z = cz + dz, y = cy + dy;
+            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
+            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
+            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
+            int w = 0;
+            for (uint32_t cb = jb; cb < je; cb += 32, w++) {
+                // bit k of the chunk's word = candidate cb + k; bits enter at the top and
+                // move down one place per candidate
+                const uint32_t ce = min(je, cb + 32u);
+                uint32_t m = 0;
 #pragma unroll 4
-            for (uint32_t j = cb; j < ce; j++) {
-                const Vec4<R> pj = ld4(pos + j);
-                const R t = h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
-                m = (m >> 1) | (t > (R) 0 ? 0x80000000u : 0u);
-                acc = poly6_acc<R>(acc, t);
+                for (uint32_t j = cb; j < ce; j++) {
+                    const Vec4<R> pj = ld4(pos + j);
+                    const R t = h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2);
+                    m = (m >> 1) | (t > (R) 0 ? 0x80000000u : 0u);
+                    acc = poly6_acc<R>(acc, t);
+                }
+                m >>= 32 - (ce - cb);
+                if (w < St::WORDS) masks[(size_t) (r * St::WORDS + w) * n + i] = m;
             }
-            m >>= 32 - (ce - cb);
-            if (w < St::WORDS) masks[(size_t) (r * St::WORDS + w) * n + i] = m;
         }
     }
     const R rho = rmul(rmul(acc, c.c_poly6), c.mass);
@@ -455,45 +464,6 @@ __device__ __forceinline__ void density_mask_one(uint32_t i, const Vec4<R> *__re
         st4(frec + 2 * (size_t) i, Vec4<R>{pi.x, pi.y, pi.z, q});
         st4(frec + 2 * (size_t) i + 1, Vec4<R>{vi.x, vi.y, vi.z, inv});
     }
-}
-
-template <class R, bool REC, int RAD = 1>
-__global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
-                                                      const uint32_t *__restrict__ start,
-                                                      const SceneDev *__restrict__ scenes, uint32_t n, Consts<R> c,
-                                                      uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ vel,
-                                                      Vec4<R> *__restrict__ frec)
-{
-    density_mask_one<R, REC, RAD>(blockIdx.x * blockDim.x + threadIdx.x, pos, aux, start, scenes, n, c, masks, vel,
-                                  frec);
-}
-
-// Persistent forms of the neighbour passes: as many resident blocks as fit on the GPU, each
-// taking the next tile of BLOCK consecutive particles from a counter until none is left, so that
-// SMs that finish their tiles early (sparse regions, small scenes of a batch) take more. The
-// counter (tiles[0]) is zeroed before each launch. Same per-particle work and bits as the flat
-// launches.
-__device__ __forceinline__ bool next_tile(uint32_t *__restrict__ tiles, uint32_t &tile)
-{
-    __shared__ uint32_t t;
-    if (threadIdx.x == 0) t = atomicAdd(tiles, 1u);
-    __syncthreads();
-    tile = t;
-    __syncthreads();
-    return true;
-}
-
-template <class R, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_density_mask_persist(const Vec4<R> *__restrict__ pos, Vec4<R> *__restrict__ aux,
-                                                                const uint32_t *__restrict__ start,
-                                                                const SceneDev *__restrict__ scenes, uint32_t n,
-                                                                Consts<R> c, uint32_t *__restrict__ masks,
-                                                                const Vec4<R> *__restrict__ vel,
-                                                                Vec4<R> *__restrict__ frec, uint32_t *__restrict__ tiles)
-{
-    uint32_t tile;
-    while (next_tile(tiles, tile) && (uint64_t) tile * BLOCK < n)
-        density_mask_one<R, true, 1>(tile * BLOCK + threadIdx.x, pos, aux, start, scenes, n, c, masks, vel, frec);
 }
 
 // Forces driven by the density pass's masks: only accepted neighbours are visited, in the
@@ -563,15 +533,16 @@ __global__ void __launch_bounds__(256, MINB) k_forces_mask(
 // loaded before either's terms are added, so two gathers are in flight at once and the loop
 // overhead is paid once per pair. The terms are still added one neighbour at a time in
 // candidate order (the sums are the same bits as the other forms of the same cell multiple).
-template <class R, bool REC, int RAD>
-__device__ __forceinline__ void forces_mask2_one(
-    uint32_t i, const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
+template <class R, int MINB, bool REC, int BLOCK = 256, int RAD = 1>
+__global__ void __launch_bounds__(BLOCK, MINB) k_forces_mask2(
+    const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
     const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
-    uint32_t n, const Consts<R> &c, const uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ frec,
+    uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ frec,
     Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out,
     uint2 *__restrict__ cid_out, uint32_t *__restrict__ count)
 {
     using St = Stencil<RAD>;
+    const uint32_t i = blockIdx.x * BLOCK + threadIdx.x;
     if (i >= n) return;
     const Vec4<R> pi = ld4(pos + i);
     const Vec4<R> vi = ld4(vel + i);
@@ -581,55 +552,63 @@ __device__ __forceinline__ void forces_mask2_one(
     hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
     const R h2 = c.h2, qi = ai.z;
     R fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
+    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
+    const int xl = cx - RAD > 0 ? cx - RAD : 0, xh = cx + RAD < X ? cx + RAD : X - 1;
 #pragma unroll 1
-    for (int r = 0; r < St::ROWS; r++) {
-        uint32_t jb, je;
-        if (!stencil_row<RAD>(sc, start, cx, cy, cz, r, jb, je)) continue;
-        if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
-        const uint32_t nw = (je - jb + 31) / 32;
-        // the row's recorded words loaded together at the start of the row
-        const uint32_t *mr = masks + (size_t) (r * St::WORDS) * n + i;
-        uint32_t wr[St::WORDS];
+    for (int dz = -RAD; dz <= RAD; dz++) {
+#pragma unroll 1
+        for (int dy = -RAD; dy <= RAD; dy++) {
+            const int r = (dz + RAD) * (2 * RAD + 1) + (dy + RAD);
+            const int z = cz + dz, y = cy + dy;
+            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
+            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
+            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
+            const uint32_t nw = (je - jb + 31) / 32;
+            // the row's recorded words loaded together at the start of the row
+            const uint32_t *mr = masks + (size_t) (r * St::WORDS) * n + i;
+            uint32_t wr[St::WORDS];
 #pragma unroll
-        for (int k = 0; k < St::WORDS; k++) wr[k] = nw > (uint32_t) k ? __ldg(mr + k * (size_t) n) : 0u;
-        for (uint32_t w = 0; w < nw; w++) {
-            const uint32_t cb = jb + 32 * w;
-            uint32_t m = 0;
-            if (w < (uint32_t) St::WORDS) {
-                m = wr[0];
+            for (int k = 0; k < St::WORDS; k++) wr[k] = nw > (uint32_t) k ? __ldg(mr + k * (size_t) n) : 0u;
+            for (uint32_t w = 0; w < nw; w++) {
+                const uint32_t cb = jb + 32 * w;
+                uint32_t m = 0;
+                if (w < (uint32_t) St::WORDS) {
+                    m = wr[0];
 #pragma unroll
-                for (int k = 1; k < St::WORDS; k++) m = w == (uint32_t) k ? wr[k] : m;
-            } else {  // beyond the recorded chunks: test the candidates here
-                const uint32_t ce = min(je, cb + 32u);
-                for (uint32_t j = ce; j-- > cb;) {
-                    const Vec4<R> pj = ld4(pos + j);
-                    m = (m << 1) | (h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2) > (R) 0 ? 1u : 0u);
+                    for (int k = 1; k < St::WORDS; k++) m = w == (uint32_t) k ? wr[k] : m;
+                } else {  // beyond the recorded chunks: test the candidates here
+                    const uint32_t ce = min(je, cb + 32u);
+                    for (uint32_t j = ce; j-- > cb;) {
+                        const Vec4<R> pj = ld4(pos + j);
+                        m = (m << 1) | (h2_minus_r2<R>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, h2) > (R) 0 ? 1u : 0u);
+                    }
                 }
-            }
-            if (i - cb < 32u) m &= ~(1u << (i - cb));  // the particle itself
-            while (m) {
-                const uint32_t j0 = cb + (uint32_t) (__ffs(m) - 1);
-                m &= m - 1;
-                const bool two = m != 0;
-                const uint32_t j1 = two ? cb + (uint32_t) (__ffs(m) - 1) : j0;
-                m &= m - 1;
-                if (!sph_check(j0 < je && j1 < je, CHK_NEIGHBOUR)) continue;
-                Vec4<R> p0, v0, p1, v1;
-                R q0, inv0, q1, inv1;
-                if (REC) {
-                    p0 = ld4(frec + 2 * (size_t) j0);
-                    v0 = ld4(frec + 2 * (size_t) j0 + 1);
-                    p1 = ld4(frec + 2 * (size_t) j1);
-                    v1 = ld4(frec + 2 * (size_t) j1 + 1);
-                    q0 = p0.w, inv0 = v0.w, q1 = p1.w, inv1 = v1.w;
-                } else {
-                    p0 = ld4(pos + j0), v0 = ld4(vel + j0);
-                    p1 = ld4(pos + j1), v1 = ld4(vel + j1);
-                    ld_qinv(aux + j0, q0, inv0);
-                    ld_qinv(aux + j1, q1, inv1);
+                if (i - cb < 32u) m &= ~(1u << (i - cb));  // the particle itself
+                while (m) {
+                    const uint32_t j0 = cb + (uint32_t) (__ffs(m) - 1);
+                    m &= m - 1;
+                    const bool two = m != 0;
+                    const uint32_t j1 = two ? cb + (uint32_t) (__ffs(m) - 1) : j0;
+                    m &= m - 1;
+                    if (!sph_check(j0 < je && j1 < je, CHK_NEIGHBOUR)) continue;
+                    Vec4<R> p0, v0, p1, v1;
+                    R q0, inv0, q1, inv1;
+                    if (REC) {
+                        p0 = ld4(frec + 2 * (size_t) j0);
+                        v0 = ld4(frec + 2 * (size_t) j0 + 1);
+                        p1 = ld4(frec + 2 * (size_t) j1);
+                        v1 = ld4(frec + 2 * (size_t) j1 + 1);
+                        q0 = p0.w, inv0 = v0.w, q1 = p1.w, inv1 = v1.w;
+                    } else {
+                        p0 = ld4(pos + j0), v0 = ld4(vel + j0);
+                        p1 = ld4(pos + j1), v1 = ld4(vel + j1);
+                        ld_qinv(aux + j0, q0, inv0);
+                        ld_qinv(aux + j1, q1, inv1);
+                    }
+                    pair_terms<R>(pi, vi, qi, p0, v0, q0, inv0, c, fpx, fpy, fpz, fvx, fvy, fvz);
+                    if (two) pair_terms<R>(pi, vi, qi, p1, v1, q1, inv1, c, fpx, fpy, fpz, fvx, fvy, fvz);
                 }
-                pair_terms<R>(pi, vi, qi, p0, v0, q0, inv0, c, fpx, fpy, fpz, fvx, fvy, fvz);
-                if (two) pair_terms<R>(pi, vi, qi, p1, v1, q1, inv1, c, fpx, fpy, fpz, fvx, fvy, fvz);
             }
         }
     }
@@ -637,32 +616,6 @@ __device__ __forceinline__ void forces_mask2_one(
     const SceneDev sc2 = load_scene(scenes, wbits(pi.w));
     finish_particle<R>(i, pi, vi, ai.x, sc2, obstacles, c, fpx, fpy, fpz, fvx, fvy, fvz, pos_out, vel_out, acc_out,
                        cid_out, count);
-}
-
-template <class R, int MINB, bool REC, int BLOCK = 256, int RAD = 1>
-__global__ void __launch_bounds__(BLOCK, MINB) k_forces_mask2(
-    const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
-    const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
-    uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ frec,
-    Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out,
-    uint2 *__restrict__ cid_out, uint32_t *__restrict__ count)
-{
-    forces_mask2_one<R, REC, RAD>(blockIdx.x * BLOCK + threadIdx.x, pos, vel, aux, start, scenes, obstacles, n, c,
-                                  masks, frec, pos_out, vel_out, acc_out, cid_out, count);
-}
-
-template <class R, int MINB, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, MINB) k_forces_mask2_persist(
-    const Vec4<R> *__restrict__ pos, const Vec4<R> *__restrict__ vel, const Vec4<R> *__restrict__ aux,
-    const uint32_t *__restrict__ start, const SceneDev *__restrict__ scenes, const ObstacleDev *__restrict__ obstacles,
-    uint32_t n, Consts<R> c, const uint32_t *__restrict__ masks, const Vec4<R> *__restrict__ frec,
-    Vec4<R> *__restrict__ pos_out, Vec4<R> *__restrict__ vel_out, Vec4<R> *__restrict__ acc_out,
-    uint2 *__restrict__ cid_out, uint32_t *__restrict__ count, uint32_t *__restrict__ tiles)
-{
-    uint32_t tile;
-    while (next_tile(tiles, tile) && (uint64_t) tile * BLOCK < n)
-        forces_mask2_one<R, true, 1>(tile * BLOCK + threadIdx.x, pos, vel, aux, start, scenes, obstacles, n, c, masks,
-                                     frec, pos_out, vel_out, acc_out, cid_out, count);
 }
 
 // All-pairs forms, the reference's brute-force simulator (sph_brute.cl:9-57) restated: every
@@ -948,19 +901,6 @@ __global__ void k_stats_final(const double *__restrict__ partial, const uint32_t
 // ------------------------------------------------------------------------------------
 static inline unsigned nblk(uint32_t n, unsigned t) { return (unsigned) ((n + t - 1) / t); }
 
-// Grid of a persistent launch: as many blocks as are resident at once on the current device.
-template <class K>
-static unsigned resident_grid(K kernel, int block)
-{
-    int dev = 0, sms = 0, per = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, 0) != cudaSuccess || per < 1 || sms < 1) {
-        cudaGetLastError();
-        return 1024;  // any grid is correct: the tiles are fetched until none is left
-    }
-    return (unsigned) (sms * per);
-}
-
 template <class R>
 cudaError_t Launch<R>::ingest(const DevBufs &b, const float *xyz, const float *vel, uint32_t first, uint32_t n,
                               int32_t scene, uint32_t id0, uint32_t nscenes, Consts<R> c, cudaStream_t st)
@@ -1013,14 +953,6 @@ cudaError_t Launch<R>::density(const DevBufs &b, uint32_t n, Consts<R> c, const 
     Vec4<R> *aux = (Vec4<R> *) b.aux;
     if (t.density_p == Tune::ALL_PAIRS) {
         k_density_all<R><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c);
-        return cudaGetLastError();
-    }
-    if (t.forces_mode == 12) {  // persistent launch over tiles of 256 particles
-        if (t.cell_mult != 1) return cudaErrorInvalidValue;
-        cudaError_t e = cudaMemsetAsync(b.tiles, 0, 4, st);
-        if (e != cudaSuccess) return e;
-        k_density_mask_persist<R, 256><<<resident_grid(k_density_mask_persist<R, 256>, 256), 256, 0, st>>>(
-            pos, aux, b.start, b.scenes, n, c, b.masks, (const Vec4<R> *) b.vel_s, (Vec4<R> *) b.frec, b.tiles);
         return cudaGetLastError();
     }
     if (t.forces_mode >= 7) {  // masks and force records
@@ -1128,14 +1060,7 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
                                                                        n, c, b.masks, (const Vec4<R> *) b.frec, po, vo,
                                                                        ao, b.cid_u, b.count);
         break;
-    case 12: {  // variant 10's kernel as a persistent launch over tiles of 128 particles
-        cudaError_t e = cudaMemsetAsync(b.tiles + 1, 0, 4, st);
-        if (e != cudaSuccess) return e;
-        k_forces_mask2_persist<R, 12, 128><<<resident_grid(k_forces_mask2_persist<R, 12, 128>, 128), 128, 0, st>>>(
-            pos, vel, aux, b.start, b.scenes, b.obstacles, n, c, b.masks, (const Vec4<R> *) b.frec, po, vo, ao, b.cid_u,
-            b.count, b.tiles + 1);
-        break;
-    }
+
     case 1:
         k_forces_list<R, 32, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
                                                                   po, vo, ao, b.cid_u, b.count);

@@ -128,28 +128,36 @@ __global__ void __launch_bounds__(128) k_density_mixed(const Vec4<float> *__rest
     int cx, cy, cz;
     hash_cell<float>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
     float sum = 0.0f, comp = 0.0f;
+    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
+    const int xl = cx - RAD > 0 ? cx - RAD : 0, xh = cx + RAD < X ? cx + RAD : X - 1;
 #pragma unroll 1
-    for (int r = 0; r < St::ROWS; r++) {
-        uint32_t jb, je;
-        if (!stencil_row<RAD>(sc, start, cx, cy, cz, r, jb, je)) continue;
-        if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
-        int w = 0;
-        for (uint32_t cb = jb; cb < je; cb += 32, w++) {
-            // bit k of the chunk's word = candidate cb + k (bits enter at the top)
-            const uint32_t ce = min(je, cb + 32u);
-            uint32_t m = 0;
-            float csum = 0.0f;  // the chunk's terms (at most 32), then one compensated add
-#pragma unroll 4
-            for (uint32_t j = cb; j < ce; j++) {
-                float x, yy, zz;
-                code_delta(gi, __ldg(gpos + j), x, yy, zz);
-                const float t = h2_minus_r2<float>(x, yy, zz, QH2);
-                m = (m >> 1) | (t > 0.0f ? 0x80000000u : 0u);
-                csum = poly6_acc<float>(csum, t);
+    for (int dz = -RAD; dz <= RAD; dz++) {
+#pragma unroll 1
+        for (int dy = -RAD; dy <= RAD; dy++) {
+            const int r = (dz + RAD) * (2 * RAD + 1) + (dy + RAD);
+            const int z = cz + dz, y = cy + dy;
+            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
+            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
+            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
+            int w = 0;
+            for (uint32_t cb = jb; cb < je; cb += 32, w++) {
+                // bit k of the chunk's word = candidate cb + k (bits enter at the top)
+                const uint32_t ce = min(je, cb + 32u);
+                uint32_t m = 0;
+                float csum = 0.0f;  // the chunk's terms (at most 32), then one compensated add
+    #pragma unroll 4
+                for (uint32_t j = cb; j < ce; j++) {
+                    float x, yy, zz;
+                    code_delta(gi, __ldg(gpos + j), x, yy, zz);
+                    const float t = h2_minus_r2<float>(x, yy, zz, QH2);
+                    m = (m >> 1) | (t > 0.0f ? 0x80000000u : 0u);
+                    csum = poly6_acc<float>(csum, t);
+                }
+                kahan_add(sum, comp, csum);
+                m >>= 32 - (ce - cb);
+                if (w < St::WORDS) masks[(size_t) (r * St::WORDS + w) * n + i] = m;
             }
-            kahan_add(sum, comp, csum);
-            m >>= 32 - (ce - cb);
-            if (w < St::WORDS) masks[(size_t) (r * St::WORDS + w) * n + i] = m;
         }
     }
     const float rho = __fmul_rn(__fmul_rn(sum, mc.poly6_q), c.mass);
@@ -210,43 +218,51 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_forces_mixed(
     const float qs = ai.z * Q_SCALE;
     float fpx = 0, fpy = 0, fpz = 0, fvx = 0, fvy = 0, fvz = 0;
     using St = Stencil<RAD>;
+    const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
+    const int xl = cx - RAD > 0 ? cx - RAD : 0, xh = cx + RAD < X ? cx + RAD : X - 1;
 #pragma unroll 1
-    for (int r = 0; r < St::ROWS; r++) {
-        uint32_t jb, je;
-        if (!stencil_row<RAD>(sc, start, cx, cy, cz, r, jb, je)) continue;
-        if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
-        const uint32_t nw = (je - jb + 31) / 32;
-        // the row's recorded words loaded together at the start of the row
-        const uint32_t *mr = masks + (size_t) (r * St::WORDS) * n + i;
-        uint32_t wr[St::WORDS];
+    for (int dz = -RAD; dz <= RAD; dz++) {
+#pragma unroll 1
+        for (int dy = -RAD; dy <= RAD; dy++) {
+            const int r = (dz + RAD) * (2 * RAD + 1) + (dy + RAD);
+            const int z = cz + dz, y = cy + dy;
+            if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
+            const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
+            const uint32_t jb = __ldg(start + row + xl), je = __ldg(start + row + xh + 1);
+            if (!sph_check(jb <= je && je <= n, CHK_ROW)) continue;
+            const uint32_t nw = (je - jb + 31) / 32;
+            // the row's recorded words loaded together at the start of the row
+            const uint32_t *mr = masks + (size_t) (r * St::WORDS) * n + i;
+            uint32_t wr[St::WORDS];
 #pragma unroll
-        for (int k = 0; k < St::WORDS; k++) wr[k] = nw > (uint32_t) k ? __ldg(mr + k * (size_t) n) : 0u;
-        for (uint32_t w = 0; w < nw; w++) {
-            const uint32_t cb = jb + 32 * w;
-            uint32_t m = 0;
-            if (w < (uint32_t) St::WORDS) {
-                m = wr[0];
+            for (int k = 0; k < St::WORDS; k++) wr[k] = nw > (uint32_t) k ? __ldg(mr + k * (size_t) n) : 0u;
+            for (uint32_t w = 0; w < nw; w++) {
+                const uint32_t cb = jb + 32 * w;
+                uint32_t m = 0;
+                if (w < (uint32_t) St::WORDS) {
+                    m = wr[0];
 #pragma unroll
-                for (int k = 1; k < St::WORDS; k++) m = w == (uint32_t) k ? wr[k] : m;
-            } else {  // beyond the recorded chunks: test the candidates here
-                const uint32_t ce = min(je, cb + 32u);
-                for (uint32_t j = ce; j-- > cb;) {
-                    float x, yy, zz;
-                    code_delta(gi, __ldg(gpos + j), x, yy, zz);
-                    m = (m << 1) | (h2_minus_r2<float>(x, yy, zz, QH2) > 0.0f ? 1u : 0u);
+                    for (int k = 1; k < St::WORDS; k++) m = w == (uint32_t) k ? wr[k] : m;
+                } else {  // beyond the recorded chunks: test the candidates here
+                    const uint32_t ce = min(je, cb + 32u);
+                    for (uint32_t j = ce; j-- > cb;) {
+                        float x, yy, zz;
+                        code_delta(gi, __ldg(gpos + j), x, yy, zz);
+                        m = (m << 1) | (h2_minus_r2<float>(x, yy, zz, QH2) > 0.0f ? 1u : 0u);
+                    }
                 }
-            }
-            if (i - cb < 32u) m &= ~(1u << (i - cb));  // the particle itself
-            while (m) {
-                const uint32_t j0 = cb + (uint32_t) (__ffs(m) - 1);
-                m &= m - 1;
-                const bool two = m != 0;
-                const uint32_t j1 = two ? cb + (uint32_t) (__ffs(m) - 1) : j0;
-                m &= m - 1;
-                if (!sph_check(j0 < je && j1 < je, CHK_NEIGHBOUR)) continue;
-                const uint4 r0 = __ldg(rec + j0), r1 = __ldg(rec + j1);
-                mixed_pair(gi, vi, qs, r0, mc, fpx, fpy, fpz, fvx, fvy, fvz);
-                if (two) mixed_pair(gi, vi, qs, r1, mc, fpx, fpy, fpz, fvx, fvy, fvz);
+                if (i - cb < 32u) m &= ~(1u << (i - cb));  // the particle itself
+                while (m) {
+                    const uint32_t j0 = cb + (uint32_t) (__ffs(m) - 1);
+                    m &= m - 1;
+                    const bool two = m != 0;
+                    const uint32_t j1 = two ? cb + (uint32_t) (__ffs(m) - 1) : j0;
+                    m &= m - 1;
+                    if (!sph_check(j0 < je && j1 < je, CHK_NEIGHBOUR)) continue;
+                    const uint4 r0 = __ldg(rec + j0), r1 = __ldg(rec + j1);
+                    mixed_pair(gi, vi, qs, r0, mc, fpx, fpy, fpz, fvx, fvy, fvz);
+                    if (two) mixed_pair(gi, vi, qs, r1, mc, fpx, fpy, fpz, fvx, fvy, fvz);
+                }
             }
         }
     }

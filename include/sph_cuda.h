@@ -210,7 +210,7 @@ int sph_get_variant(const sph_ctx *ctx, int32_t out[2]);
  * order). The plain FP32 and mixed forms only (SPH_ERR_UNSUPPORTED for FP64 and all-pairs);
  * between steps only (SPH_ERR_STATE between passes). sph_get_grid still reports the reference's
  * grid of cells of size h. sph_get_cell_multiple returns the current multiple (or SPH_ERR_ARG).
- * The autotuner chooses the multiple with the variants. */
+ * The autotuner chooses the multiple with the variants, unless it was set here. */
 int sph_set_cell_multiple(sph_ctx *ctx, int32_t cell_multiple);
 int sph_get_cell_multiple(const sph_ctx *ctx);
 

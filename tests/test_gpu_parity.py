@@ -611,12 +611,14 @@ def test_splat_counts_and_depth(sphlib, tmp_path):
 
 
 def test_online_tuning_keeps_the_bits(sphlib):
-    """Online tuning switches force variants between real steps; the run is bit-identical to
-    one without it, through sph_step (graphs between trials) and through the pass calls."""
+    """Online tuning switches force variants between real steps; with the cell multiple set by
+    the caller (so that it stays) the run is bit-identical to one without online tuning, through
+    sph_step (graphs between trials) and through the pass calls."""
     pos = c0_scene(sphlib, dims=(16, 16, 16))
     runs = []
     for mode in ("plain", "online_step", "online_passes"):
         ctx = sphlib.SphContext(C0_BOX, pos.shape[0], gravity=G981, flags=sphlib.SPH_FLAG_RECORD_ACC)
+        ctx.set_cell_multiple(1)
         ctx.upload(pos)
         ctx.set_variant(0, 4)
         if mode != "plain":
@@ -644,6 +646,7 @@ def test_online_tuning_keeps_the_bits(sphlib):
     for mode in ("fixed", "online_step", "online_passes"):
         m = sphlib.SphContext(C0_BOX, pos.shape[0], precision=sphlib.SPH_MIXED, gravity=G981,
                               flags=sphlib.SPH_FLAG_RECORD_ACC)
+        m.set_cell_multiple(1)
         m.upload(pos)
         m.set_variant(0, 0)
         if mode != "fixed":
@@ -668,6 +671,37 @@ def test_online_tuning_keeps_the_bits(sphlib):
         m.set_variant(0, 4)  # the mixed form has force variants 0-3 only
     assert e.value.code == sphlib.SPH_ERR_ARG
     m.close()
+
+
+@pytest.mark.parametrize("prec", ["plain", "mixed"])
+def test_online_tuning_across_cell_multiples(sphlib, oracle_mod, prec):
+    """Unpinned, online tuning also tries the other cell multiple once per period and keeps the
+    faster grid: every step still matches the oracle's step from the same state (plain: the 1e-5
+    band; mixed: density within 1e-3 of the FP64 run), whichever grid ran it."""
+    box, pos, vel, g = scenes(sphlib, oracle_mod)["c0_8000_moving"]
+    form = {"plain": sphlib.SPH_PLAIN_F32, "mixed": sphlib.SPH_MIXED}[prec]
+    ctx = sphlib.SphContext(box, pos.shape[0], precision=form, gravity=g, flags=sphlib.SPH_FLAG_RECORD_ACC)
+    ctx.upload(pos, vel)
+    ctx.set_online_tuning(4)
+    seen = set()
+    for k in range(12):
+        cur = ctx.download()
+        if k % 2:
+            ctx.pass_grid()
+            ctx.pass_density()
+            ctx.pass_forces()
+        else:
+            ctx.step(1)
+        got = ctx.download(acc=True)
+        seen.add(ctx.cell_multiple())
+        if prec == "plain":
+            ref = oracle_run(oracle_mod, box, cur["pos"], cur["vel"], gravity=g)
+            assert_within(rel_errors(got, ref), f"online step {k}")
+        else:
+            ref = gpu_run(sphlib, box, cur["pos"], cur["vel"], precision=sphlib.SPH_F64, gravity=g)
+            assert np.max(np.abs(got["rho"] - ref["rho"]) / ref["rho"]) < 1e-3, k
+    assert seen <= {1, 2}
+    ctx.close()
 
 
 def test_pinned_transfers_equal_staged_transfers(sphlib):
