@@ -258,12 +258,16 @@ def timed_run(ctx, torch, ext, flush, warmup, k, run, on_step=None):
     """Steps a context through `warmup` untimed steps and then a `run`-step run of which the k
     steps of timed_steps(k, run) are timed: per timed step, L2 flushed, then the three passes
     between CUDA events on the library's stream. Returns the per-step event times
-    [(grid, density, forces), ...] and the force variant of each timed step."""
+    [(grid, density, forces), ...] and the (force variant, cell multiple) of each timed step
+    (read after the step's grid pass: online tuning may change both between steps)."""
+    chosen = []
+
     def passes(evs=None):
         if evs is not None:
             evs[0].record(ext)
         ctx.pass_grid()
         if evs is not None:
+            chosen.append((ctx.variant()[1], ctx.cell_multiple()))
             evs[1].record(ext)
         ctx.pass_density()
         if evs is not None:
@@ -288,7 +292,7 @@ def timed_run(ctx, torch, ext, flush, warmup, k, run, on_step=None):
             e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
             passes(e)
             evs.append(e)
-            used.append(ctx.variant()[1])
+            used.append(chosen[-1])
         else:
             passes()
     torch.cuda.synchronize()
@@ -310,10 +314,10 @@ def mixed_leg(sphcuda, torch, pos, vel0, steps, warmup, flush, dev, run=RUN_STEP
     ctx.autotune(reps=3)
     ctx.set_online_tuning(50)
     ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
-    times, _ = timed_run(ctx, torch, ext, flush, warmup, steps, max(steps, run))
+    times, used = timed_run(ctx, torch, ext, flush, warmup, steps, max(steps, run))
     total_ms = sum(sum(t) for t in times)
     check = fp64_error(sphcuda, ctx, sphcuda.SPH_MIXED, N)
-    check["cell_multiple"] = ctx.cell_multiple()
+    check["cell_multiple_steps"] = {str(m): sum(1 for u in used if u[1] == m) for m in (1, 2)}
     check["passes_ms"] = {k: sum(t[q] for t in times) / len(times) for q, k in enumerate(("grid", "density", "forces"))}
     ctx.close()
     return N * len(times) / (total_ms / 1000.0), total_ms / len(times), check
@@ -362,7 +366,8 @@ def batch_leg(sphcuda, torch, steps, warmup, flush, dev):
         times, used = timed_run(ctx, torch, ext, flush, warmup, steps, max(steps, BATCH_RUN_STEPS))
         total_ms = sum(sum(t) for t in times)
         res[name] = {"value": N * len(times) / (total_ms / 1000.0), "ms_per_step": total_ms / len(times),
-                     "cell_multiple": ctx.cell_multiple(), "forces_variants": sorted(set(used)),
+                     "cell_multiple_steps": {str(m): sum(1 for u in used if u[1] == m) for m in (1, 2)},
+                     "forces_variants": sorted({u[0] for u in used}),
                      "passes_ms": {k: sum(t[q] for t in times) / len(times)
                                    for q, k in enumerate(("grid", "density", "forces"))},
                      "rho_max_rel_vs_fp64": batch_fp64_error(sphcuda, ctx, prec, boxes, counts)}
@@ -726,11 +731,12 @@ def main():
     mean = lambda xs: sum(xs) / len(xs)
     dom = "forces" if mean(forc_ms) >= mean(dens_ms) else "density"
     dom_ms = mean(forc_ms) if dom == "forces" else mean(dens_ms)
-    main_v = max(set(used), key=used.count)
+    vs = [u[0] for u in used]
+    main_v = max(set(vs), key=vs.count)
     # compulsory bytes (the roofline) and the implementation's own bytes, by the variant each
     # timed step ran
     comp = compulsory_bytes(N, C, args.form)
-    ab_steps = [alg_bytes(N, C, rs, v) for v in used]
+    ab_steps = [alg_bytes(N, C, rs, v) for v, _ in used]
     ab = {k: sum(a[k] for a in ab_steps) / len(ab_steps) for k in ab_steps[0]}
     achieved = comp[dom] / (dom_ms / 1000.0) / 1e9
     impl_achieved = ab[dom] / (dom_ms / 1000.0) / 1e9
@@ -828,8 +834,9 @@ def main():
         "batch": batch,
         "cpu_baseline": cpu,
         "gpu_launches": KERNELS_PER_STEP * K,
-        "launch_variant": {"density": variant[0], "forces": main_v, "cell_multiple": cell_mult,
-                           "forces_steps": {str(v): used.count(v) for v in sorted(set(used))},
+        "launch_variant": {"density": variant[0], "forces": main_v, "cell_multiple_at_start": cell_mult,
+                           "forces_steps": {str(v): vs.count(v) for v in sorted(set(vs))},
+                           "cell_multiple_steps": {str(m): sum(1 for u in used if u[1] == m) for m in (1, 2)},
                            "picked_by": "--variant" if args.variant else
                            "sph_autotune (cell multiple and variants), then online tuning every 50 steps"},
         "clocks": clk,

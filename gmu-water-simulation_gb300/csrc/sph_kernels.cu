@@ -1061,6 +1061,7 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
                                                                        ao, b.cid_u, b.count);
         break;
 
+
     case 1:
         k_forces_list<R, 32, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
                                                                   po, vo, ao, b.cid_u, b.count);
