@@ -131,11 +131,16 @@ MASK_BYTES = 36  # 9 rows x one 32-bit mask word per particle (rest density)
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) and warp instructions
 # (smsp__inst_executed.sum) per launch of the dominant kernels in the compressed column (step ~254
 # of this workload, where most of the run is spent), one ncu capture of each kernel alone with
-# force variant 10: profiles/k_forces_mask2_variant10_k_density_mask_step254_dam_break_1m.md
-TRAFFIC = {"k_forces": 194.83e6, "k_density": 102.56e6}
-ISSUE = {"k_forces": 388.12e6, "k_density": 312.25e6}
-TRAFFIC_SOURCE = ("ncu, one launch at step ~254 (the compressed column), force variant 10: "
-                  "profiles/k_forces_mask2_variant10_k_density_mask_step254_dam_break_1m.md")
+# force variant 10, keyed by (kernel, cell multiple):
+# profiles/k_forces_mask2_variant10_k_density_mask_step254_dam_break_1m.md (cells of h) and
+# profiles/k_forces_mask2_k_density_mask_half_cells_step254_dam_break_1m.md (cells of h/2)
+TRAFFIC = {("k_forces", 1): 194.83e6, ("k_density", 1): 102.56e6,
+           ("k_forces", 2): 210.24e6, ("k_density", 2): 117.41e6}
+ISSUE = {("k_forces", 1): 388.12e6, ("k_density", 1): 312.25e6,
+         ("k_forces", 2): 300.82e6, ("k_density", 2): 261.00e6}
+TRAFFIC_SOURCE = ("ncu, one launch at step ~254 (the compressed column), force variant 10, on the run's "
+                  "main cell multiple: profiles/k_forces_mask2_variant10_k_density_mask_step254_dam_break_1m.md, "
+                  "profiles/k_forces_mask2_k_density_mask_half_cells_step254_dam_break_1m.md")
 ISSUE_SOURCE = TRAFFIC_SOURCE
 
 
@@ -740,8 +745,10 @@ def main():
     ab = {k: sum(a[k] for a in ab_steps) / len(ab_steps) for k in ab_steps[0]}
     achieved = comp[dom] / (dom_ms / 1000.0) / 1e9
     impl_achieved = ab[dom] / (dom_ms / 1000.0) / 1e9
-    traffic = TRAFFIC.get(f"k_{dom}") if args.form == "plain" else None
-    inst = ISSUE.get(f"k_{dom}") if args.form == "plain" else None
+    ms_ = [u[1] for u in used]
+    main_m = max(set(ms_), key=ms_.count)  # the cell multiple most timed steps ran on
+    traffic = TRAFFIC.get((f"k_{dom}", main_m)) if args.form == "plain" else None
+    inst = ISSUE.get((f"k_{dom}", main_m)) if args.form == "plain" else None
     sm_mhz = clk.get("sm_mhz") or 2070.0
     issue = None
     if inst:

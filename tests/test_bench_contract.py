@@ -37,7 +37,8 @@ def test_byte_model_matches_the_documented_totals():
         ab = bench.alg_bytes(N, C, 4, v)
         assert ab["density"] == 116 * N + 4 * C and ab["forces"] == 156 * N + 12 * C
         assert sum(ab.values()) == 360 * N + 48 * C
-    assert set(bench.TRAFFIC) == {"k_forces", "k_density"} and set(bench.ISSUE) == set(bench.TRAFFIC)
+    keys = {(k, m) for k in ("k_forces", "k_density") for m in (1, 2)}
+    assert set(bench.TRAFFIC) == keys and set(bench.ISSUE) == keys
 
 
 def test_reference_arm_loads_no_product_library():
