@@ -111,10 +111,10 @@ def alg_bytes(N, C, rs=4, forces_variant=4):
     r4 = 4 * rs
     rec = 3 * r4 * N if forces_variant >= 7 else 0  # velocity read + 2 x r4 record written
     return {
-        # counts read twice, starts/cursors written, counts zeroed
-        "scan": 20 * C,
-        # (cell, id) read, id scattered, cursor read-modify-write
-        "slot": 12 * N + 8 * C,
+        # counts read twice, starts written
+        "scan": 12 * C,
+        # (cell, id) read, id scattered, cell start read, count read-modify-write (back to 0)
+        "slot": 12 * N + 12 * C,
         # (cell, id) + the cell's ids read, state read and written in sorted order, starts
         "rank_permute": 8 * N + 4 * N + 4 * r4 * N + 4 * C,
         # sorted positions read, (rho, p, p/rho^2, 1/rho) written, row starts; the mask form
@@ -610,6 +610,19 @@ def run_config(args):
     advance(max(args.warmup, 3), warm)
     ms = []
     work = advance(args.steps, ms)
+    # five more steps from the final state (the run's largest particle count), each pass between
+    # its own events; the grid pass is the scan, slot, crowded-cell sort, rank and permute
+    fin = []
+    for _ in range(5):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        for q, p in enumerate((ctx.pass_grid, ctx.pass_density, ctx.pass_forces)):
+            e[q].record(ext)
+            p()
+        e[3].record(ext)
+        fin.append(e)
+    torch.cuda.synchronize()
+    final_passes = {k: sum(e[q].elapsed_time(e[q + 1]) for e in fin) / len(fin)
+                    for q, k in enumerate(("grid", "density", "forces"))}
     st = ctx.stats(0)
     finite = bool(np.isfinite(st["rho_mean"]))
     check = config_fp64_error(sphcuda, ctx, form, boxes, obstacles) if args.fp64_check else None
@@ -618,7 +631,7 @@ def run_config(args):
             "warmup": max(args.warmup, 3), "ms_per_step": sum(ms) / args.steps,
             "launch_variant": list(ctx.variant()), "cell_multiple": ctx.cell_multiple(),
             "finite": finite, "rho_mean_scene0": st["rho_mean"], "l2": "not flushed (replayed steps)",
-            "fp64_check": check}
+            "final_passes_ms": final_passes, "fp64_check": check}
     ctx.close()
     print(json.dumps(line), flush=True)
     return 0

@@ -254,7 +254,7 @@ size_t pool_layout(sph_ctx *c, std::vector<PoolItem> &items)
         {&b.pos_s, r4 * N}, {&b.vel_s, r4 * N}, {&b.pos_u, r4 * N}, {&b.vel_u, r4 * N}, {&b.aux, r4 * N},
         {&b.acc, rec ? r4 * N : 0},
         {(void **) &b.cid_u, 8 * N}, {(void **) &b.tmp, 4 * N},
-        {(void **) &b.count, 4 * C}, {(void **) &b.start, 4 * (C + 1)}, {(void **) &b.cursor, 4 * C},
+        {(void **) &b.count, 4 * C}, {(void **) &b.start, 4 * (C + 1)},
         {(void **) &b.bsum, 4 * nb}, {(void **) &b.big, 4 * big_words(N)},
         {(void **) &b.scenes, sizeof(SceneDev) * c->sc.size()},
         {(void **) &b.obstacles, sizeof(ObstacleDev) * (nobs ? nobs : 1)},
@@ -1500,14 +1500,13 @@ int get_grid_ref(sph_ctx *c, uint32_t *cell_of_particle, uint32_t *cell_counts, 
         cmax = std::max<uint64_t>(cmax, (uint64_t) h.res[0] * h.res[1] * h.res[2]);
     }
     const uint64_t nb = cmax / kScanTile + 1;
-    const uint64_t words = nmax + (cmax + 1) + nmax + 2 * cmax + nmax + nb + big_words(nmax);
+    const uint64_t words = nmax + (cmax + 1) + nmax + cmax + nmax + nb + big_words(nmax);
     uint32_t *mem = nullptr;
     CK(c, cudaMalloc(&mem, 4 * words));
     uint32_t *d_cell = mem, *d_start = d_cell + nmax, *d_order = d_start + cmax + 1;
     GridScratch g;
     g.count = d_order + nmax;
-    g.cursor = g.count + cmax;
-    g.tmp = g.cursor + cmax;
+    g.tmp = g.count + cmax;
     g.bsum = g.tmp + nmax;
     g.big = g.bsum + nb;
     uint64_t off = 0, cbase = 0;

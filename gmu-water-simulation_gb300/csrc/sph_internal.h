@@ -54,9 +54,8 @@ struct DevBufs {
     void *pos_s, *vel_s, *pos_u, *vel_u, *aux, *acc;  // R4 arrays
     uint2 *cid_u;          // (global cell, id) of every *_u particle
     uint32_t *tmp;         // ids scattered into cell slots, for the canonical rank
-    uint32_t *count;       // particles per global cell (hash output, zeroed by the scan)
+    uint32_t *count;       // particles per global cell (hash output; the slot pass counts it back to 0)
     uint32_t *start;       // exclusive scan of count, ncells_total + 1 entries
-    uint32_t *cursor;      // running slot per cell (starts at start[c])
     uint32_t *bsum;        // scan block sums
     uint32_t *big;         // cells above kBigCell particles: count in word 0, then the cells (big_words(n) words)
     SceneDev *scenes;
@@ -208,10 +207,10 @@ cudaError_t launch_splat(const DevBufs &b, uint32_t n, int layout_sorted, uint32
                          float half_v, float scale_u, float scale_v, uint32_t width, uint32_t height,
                          uint32_t *count, float *depth, cudaStream_t st);
 
-// Working memory of a reference-grid build of n particles and C cells: counts and cursors (C
-// words each), slot ids (n), scan block sums (C / kScanTile + 1), crowded cells (big_words(n)).
+// Working memory of a reference-grid build of n particles and C cells: counts (C words), slot
+// ids (n), scan block sums (C / kScanTile + 1), crowded cells (big_words(n)).
 struct GridScratch {
-    uint32_t *count, *cursor, *tmp, *bsum, *big;
+    uint32_t *count, *tmp, *bsum, *big;
 };
 // the reference's grid (cells of size h) of n id-ordered float positions (sph_noalloc.cu)
 cudaError_t ref_grid_build(const float *xyz, uint32_t n, int3 res, float3 half, float h, uint32_t *out_cell,

@@ -66,8 +66,8 @@ __global__ void __launch_bounds__(256) k_ingest(Vec4<R> *__restrict__ pos_u, Vec
 // Exclusive scan of the per-cell counts into cell starts (per-tile sums, then per tile the
 // offset from the earlier sums and the scan of the tile).
 // Replaces scan_local / increment_local_scans (resources/kernels/sph_grid.cl:71-121, 9-23)
-// and its sums-buffer race. The apply phase also seeds the slot cursors and zeroes the
-// counts for the next hash.
+// and its sums-buffer race. The counts are left as they are: the slot pass takes every slot
+// by decrementing its cell's count, which leaves the counts at zero for the next hash.
 // 1024-cell tiles (256 threads x 4 cells, one 16-byte access per array and thread): enough
 // blocks to fill the GPU on grids of a few hundred thousand cells.
 constexpr int SCAN_THREADS = 256;
@@ -143,10 +143,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *__
     }
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t *__restrict__ count, uint32_t ncells,
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t *__restrict__ count, uint32_t ncells,
                                                              const uint32_t *__restrict__ bsum,
-                                                             uint32_t *__restrict__ start,
-                                                             uint32_t *__restrict__ cursor, bool vec,
+                                                             uint32_t *__restrict__ start, bool vec,
                                                              uint32_t *__restrict__ big)
 {
     const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
@@ -174,15 +173,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t *__restric
     }
     if (vec && base + 4 <= ncells) {
         *reinterpret_cast<uint4 *>(start + base) = st4v;
-        *reinterpret_cast<uint4 *>(cursor + base) = st4v;
-        *reinterpret_cast<uint4 *>(count + base) = make_uint4(0, 0, 0, 0);
     } else {
         const uint32_t sv[4] = {st4v.x, st4v.y, st4v.z, st4v.w};
-        for (uint32_t k = 0; k < 4 && base + k < ncells; k++) {
-            start[base + k] = sv[k];
-            cursor[base + k] = sv[k];
-            count[base + k] = 0;
-        }
+        for (uint32_t k = 0; k < 4 && base + k < ncells; k++) start[base + k] = sv[k];
     }
 }
 
@@ -192,8 +185,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t *__restric
 // a smaller id. The resulting order is ascending (cell, id) regardless of atomic order;
 // the reference leaves the within-cell order unspecified (host std::sort,
 // src/CGPUParticleSimulator.cpp:116-139; swap-remove lists, src/CCPUParticleSimulator.cpp:72-84).
+// Slots are taken from the top of each cell down: the count still unclaimed in a cell is the
+// end of its free slots, and the last slot taken returns the count to zero for the next hash.
 __global__ void __launch_bounds__(256) k_slot(const uint2 *__restrict__ cid_u, uint32_t n,
-                                              uint32_t *__restrict__ cursor, uint32_t *__restrict__ tmp)
+                                              const uint32_t *__restrict__ start, uint32_t *__restrict__ count,
+                                              uint32_t *__restrict__ tmp)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -203,8 +199,12 @@ __global__ void __launch_bounds__(256) k_slot(const uint2 *__restrict__ cid_u, u
     const unsigned lane = threadIdx.x & 31u;
     const unsigned peers = __match_any_sync(__activemask(), cd.x);
     const int leader = __ffs(peers) - 1;
+    const uint32_t take = (uint32_t) __popc(peers);
     uint32_t base = 0;
-    if ((int) lane == leader) base = atomicAdd(cursor + cd.x, (uint32_t) __popc(peers));
+    if ((int) lane == leader) {
+        const uint32_t left = atomicSub(count + cd.x, take);  // this warp takes slots left-take .. left-1
+        base = __ldg(start + cd.x) + left - take;
+    }
     base = __shfl_sync(peers, base, leader);
     const uint32_t t = base + (uint32_t) __popc(peers & ((1u << lane) - 1u));
     if (sph_check(t < n, CHK_SORT)) tmp[t] = cd.y;
@@ -915,11 +915,10 @@ template <class R>
 cudaError_t Launch<R>::scan(const DevBufs &b, uint32_t ncells, cudaStream_t st)
 {
     const uint32_t nb = (ncells + SCAN_TILE - 1) / SCAN_TILE;
-    // 16-byte accesses only where all three arrays allow them (a caller's start array may not)
-    const bool vec = ((reinterpret_cast<uintptr_t>(b.count) | reinterpret_cast<uintptr_t>(b.start) |
-                       reinterpret_cast<uintptr_t>(b.cursor)) & 15u) == 0;
+    // 16-byte accesses only where both arrays allow them (a caller's start array may not)
+    const bool vec = ((reinterpret_cast<uintptr_t>(b.count) | reinterpret_cast<uintptr_t>(b.start)) & 15u) == 0;
     k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, vec, b.big);
-    k_scan_apply<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, b.start, b.cursor, vec, b.big);
+    k_scan_apply<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, b.start, vec, b.big);
     return cudaGetLastError();
 }
 
@@ -927,7 +926,7 @@ template <class R>
 cudaError_t Launch<R>::permute(const DevBufs &b, uint32_t n, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
-    k_slot<<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.cursor, b.tmp);
+    k_slot<<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.start, b.count, b.tmp);
     cudaError_t e = launch_sort_big(b.start, b.tmp, b.big, st);
     if (e != cudaSuccess) return e;
     k_rank_permute<R><<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.start, b.tmp, (const Vec4<R> *) b.pos_u,
@@ -1113,7 +1112,7 @@ cudaError_t Launch<R>::stats(const DevBufs &b, uint32_t nscenes, Consts<R> c, in
 cudaError_t launch_slot(const DevBufs &b, uint32_t n, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
-    k_slot<<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.cursor, b.tmp);
+    k_slot<<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.start, b.count, b.tmp);
     return launch_sort_big(b.start, b.tmp, b.big, st);
 }
 

@@ -4,7 +4,7 @@
 // already handed its GPU memory to its own pool allocator, or a per-frame callback in a
 // real-time loop, where cudaMalloc/cudaFree would synchronise the device and stall the frame.
 // The caller passes device arrays for the positions and for every output; the kernels'
-// working memory (per-cell counts and cursors, per-particle slot ids, scan block sums, the list
+// working memory (per-cell counts, per-particle slot ids, scan block sums, the list
 // of crowded cells) lives in one file-scope device array of fixed size. The array belongs to
 // the library's device code: CUDA creates it on a device when that code is loaded there, which
 // under lazy module loading (the default) is the first call on that device. That first call
@@ -13,7 +13,7 @@
 // a call holds the array until the process exits. cudaDeviceReset is not supported between
 // calls: the address looked up by the first call would then be stale.
 //
-// Limits: at most kMaxParticles particles and kMaxCells grid cells per call (about 12 MiB of
+// Limits: at most kMaxParticles particles and kMaxCells grid cells per call (about 8 MiB of
 // scratch). Calls share the scratch array, which keeps the previous call's contents: each
 // call clears what must start at zero, and two calls whose work overlaps on the GPU (on
 // different streams, or from different host threads) race on it and must not be issued.
@@ -33,8 +33,8 @@ constexpr uint32_t kMaxParticles = 1u << 20;
 constexpr uint32_t kMaxCells = 1u << 20;
 constexpr uint32_t kMaxBlocks = kMaxCells / kScanTile + 1;  // scan block sums
 constexpr size_t kBigWords = big_words(kMaxParticles);       // crowded-cell list
-// counts | cursors | slot ids | scan block sums | crowded cells, as 32-bit words
-constexpr size_t kScratchWords = (size_t) kMaxCells + kMaxCells + kMaxParticles + kMaxBlocks + kBigWords;
+// counts | slot ids | scan block sums | crowded cells, as 32-bit words
+constexpr size_t kScratchWords = (size_t) kMaxCells + kMaxParticles + kMaxBlocks + kBigWords;
 
 __device__ __align__(256) uint32_t g_grid_scratch[kScratchWords];
 
@@ -58,12 +58,15 @@ __global__ void __launch_bounds__(256) k_hash_plain_xyz(const float *__restrict_
     atomicAdd(count + cell, 1u);
 }
 
+// every id takes a slot of its cell, from the top down (the counts end at zero)
 __global__ void __launch_bounds__(256) k_slot_ids(const uint32_t *__restrict__ cell, uint32_t n,
-                                                  uint32_t *__restrict__ cursor, uint32_t *__restrict__ slot_ids)
+                                                  const uint32_t *__restrict__ start, uint32_t *__restrict__ count,
+                                                  uint32_t *__restrict__ slot_ids)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    slot_ids[atomicAdd(cursor + cell[i], 1u)] = i;
+    const uint32_t c = cell[i];
+    slot_ids[start[c] + atomicSub(count + c, 1u) - 1u] = i;
 }
 
 // canonical (cell, id) order: position = cell start + number of same-cell ids below i
@@ -82,7 +85,7 @@ __global__ void __launch_bounds__(256) k_rank_ids(const uint32_t *__restrict__ c
 
 // The reference's grid of n particles (float xyz, id order) in a box of res cells per axis (cells
 // of size h, linear index x + y*X + z*X*Y): the cell of every particle, the cell starts and the
-// ids in ascending (cell, id) order, with the working memory g (counts, cursors, slot ids, scan
+// ids in ascending (cell, id) order, with the working memory g (counts, slot ids, scan
 // block sums, crowded-cell list) supplied by the caller.
 cudaError_t ref_grid_build(const float *xyz, uint32_t n, int3 res, float3 half, float h, uint32_t *out_cell,
                            uint32_t *out_start, uint32_t *out_order, const GridScratch &g, cudaStream_t st)
@@ -90,7 +93,6 @@ cudaError_t ref_grid_build(const float *xyz, uint32_t n, int3 res, float3 half, 
     const uint64_t ncells = (uint64_t) res.x * (uint64_t) res.y * (uint64_t) res.z;
     DevBufs b{};
     b.count = g.count;
-    b.cursor = g.cursor;
     b.tmp = g.tmp;
     b.bsum = g.bsum;
     b.big = g.big;
@@ -100,9 +102,9 @@ cudaError_t ref_grid_build(const float *xyz, uint32_t n, int3 res, float3 half, 
     if (e != cudaSuccess) return e;
     const unsigned blocks = (unsigned) ((n + 255) / 256);
     if (n) k_hash_plain_xyz<<<blocks, 256, 0, st>>>(xyz, n, half, res, 1.0f / h, (double) h, out_cell, b.count);
-    e = Launch<float>::scan(b, (uint32_t) ncells, st);  // starts; cursors = starts; counts back to 0
+    e = Launch<float>::scan(b, (uint32_t) ncells, st);  // starts
     if (e == cudaSuccess && n) {
-        k_slot_ids<<<blocks, 256, 0, st>>>(out_cell, n, b.cursor, b.tmp);
+        k_slot_ids<<<blocks, 256, 0, st>>>(out_cell, n, b.start, b.count, b.tmp);
         e = launch_sort_big(b.start, b.tmp, b.big, st);
         if (e == cudaSuccess) {
             k_rank_ids<<<blocks, 256, 0, st>>>(out_cell, n, b.start, b.tmp, out_order);
@@ -151,9 +153,8 @@ extern "C" int sph_grid_build_noalloc(const float *xyz, uint32_t n, const float 
     }
     GridScratch g;
     g.count = scratch;
-    g.cursor = scratch + kMaxCells;
-    g.tmp = scratch + 2 * (size_t) kMaxCells;
-    g.bsum = scratch + 2 * (size_t) kMaxCells + kMaxParticles;
+    g.tmp = scratch + (size_t) kMaxCells;
+    g.bsum = scratch + (size_t) kMaxCells + kMaxParticles;
     g.big = g.bsum + kMaxBlocks;
     const float3 half = make_float3(box[0] / 2.0f, box[1] / 2.0f, box[2] / 2.0f);
     const cudaError_t e = ref_grid_build(xyz, n, res, half, h, out_cell, out_start, out_order, g, (cudaStream_t) stream);

@@ -303,7 +303,7 @@ int sph_stats(sph_ctx *ctx, uint32_t scene, double out[8]);
  *   out_start  X*Y*Z + 1: cell starts, out_start[X*Y*Z] = n
  *   out_order  n: particle ids in ascending (cell, id) order
  * The cells and order equal the grid that sph_pass_grid builds for the same positions and h.
- * Working memory is one fixed device array of about 12 MiB inside this library, held by every
+ * Working memory is one fixed device array of about 8 MiB inside this library, held by every
  * GPU that has run a call until the process exits, so n and X*Y*Z are each limited to 1,048,576;
  * larger requests return SPH_ERR_CAPACITY, and a non-finite box or h SPH_ERR_ARG. The first call
  * on a device is its setup: CUDA creates the array there when the library's device code is
