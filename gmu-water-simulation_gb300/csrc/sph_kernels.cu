@@ -187,10 +187,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t *__r
 // src/CGPUParticleSimulator.cpp:116-139; swap-remove lists, src/CCPUParticleSimulator.cpp:72-84).
 // Slots are taken from the top of each cell down: the count still unclaimed in a cell is the
 // end of its free slots, and the last slot taken returns the count to zero for the next hash.
-// The grid kernels are bound by the latency of their dependent loads and atomics, not by their
-// bytes, so each thread carries P particles, one from each of its block's P consecutive tiles
-// of 256 (a warp still covers 32 consecutive particles per tile), and their chains overlap.
-constexpr int GRID_PER = 4;
+// The kernel is bound by the latency of its load -> atomic -> store chain, not by its bytes, so
+// each thread carries P particles, one from each of its block's P consecutive tiles of 256 (a
+// warp still covers 32 consecutive particles per tile), and the P chains overlap.
+constexpr int SLOT_PER = 4;
 constexpr uint32_t kNoCell = 0xffffffffu;  // match key of lanes past n (no cell reaches 2^31)
 
 template <int P>
@@ -264,7 +264,9 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_big(const uint32_t *__res
     }
 }
 
-template <class R, int P>
+// One particle per thread here (more per thread measured slower: the rank loop's registers cost
+// more occupancy than the overlap gains); the state loads are issued before the rank is counted.
+template <class R>
 __global__ void __launch_bounds__(256) k_rank_permute(const uint2 *__restrict__ cid_u, uint32_t n,
                                                       const uint32_t *__restrict__ start,
                                                       const uint32_t *__restrict__ tmp,
@@ -272,33 +274,16 @@ __global__ void __launch_bounds__(256) k_rank_permute(const uint2 *__restrict__ 
                                                       const Vec4<R> *__restrict__ vel_u,
                                                       Vec4<R> *__restrict__ pos_s, Vec4<R> *__restrict__ vel_s)
 {
-    uint32_t idx[P];
-    uint2 cd[P];
-    Vec4<R> p[P], v[P];
-#pragma unroll
-    for (int k = 0; k < P; k++) {
-        idx[k] = (blockIdx.x * P + k) * 256u + threadIdx.x;
-        if (idx[k] < n) {  // the state is in flight while the ranks are counted
-            cd[k] = cid_u[idx[k]];
-            p[k] = ld4(pos_u + idx[k]);
-            v[k] = ld4(vel_u + idx[k]);
-        }
-    }
-    uint32_t b[P], e[P];
-#pragma unroll
-    for (int k = 0; k < P; k++)
-        if (idx[k] < n) {
-            b[k] = start[cd[k].x];
-            e[k] = start[cd[k].x + 1];
-        }
-#pragma unroll
-    for (int k = 0; k < P; k++) {
-        if (idx[k] >= n || !sph_check(b[k] <= e[k] && e[k] <= n, CHK_SORT)) continue;
-        const uint32_t dst = b[k] + rank_in_cell(tmp, b[k], e[k], cd[k].y);
-        if (!sph_check(dst < e[k], CHK_SORT)) continue;
-        st4(pos_s + dst, p[k]);
-        st4(vel_s + dst, v[k]);
-    }
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint2 cd = cid_u[i];
+    const Vec4<R> p = ld4(pos_u + i), v = ld4(vel_u + i);
+    const uint32_t b = start[cd.x], e = start[cd.x + 1];
+    if (!sph_check(b <= e && e <= n, CHK_SORT)) return;
+    const uint32_t dst = b + rank_in_cell(tmp, b, e, cd.y);
+    if (!sph_check(dst < e, CHK_SORT)) return;
+    st4(pos_s + dst, p);
+    st4(vel_s + dst, v);
 }
 
 // ------------------------------------------------------------------------------------
@@ -962,11 +947,10 @@ template <class R>
 cudaError_t Launch<R>::permute(const DevBufs &b, uint32_t n, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
-    k_slot<GRID_PER><<<nblk(n, 256 * GRID_PER), 256, 0, st>>>(b.cid_u, n, b.start, b.count, b.tmp);
+    k_slot<SLOT_PER><<<nblk(n, 256 * SLOT_PER), 256, 0, st>>>(b.cid_u, n, b.start, b.count, b.tmp);
     cudaError_t e = launch_sort_big(b.start, b.tmp, b.big, st);
     if (e != cudaSuccess) return e;
-    constexpr int PR = sizeof(R) == 4 ? GRID_PER : GRID_PER / 2;  // FP64 state: twice the registers per particle
-    k_rank_permute<R, PR><<<nblk(n, 256 * PR), 256, 0, st>>>(b.cid_u, n, b.start, b.tmp, (const Vec4<R> *) b.pos_u,
+    k_rank_permute<R><<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.start, b.tmp, (const Vec4<R> *) b.pos_u,
                                                     (const Vec4<R> *) b.vel_u, (Vec4<R> *) b.pos_s,
                                                     (Vec4<R> *) b.vel_s);
     return cudaGetLastError();
@@ -1149,7 +1133,7 @@ cudaError_t Launch<R>::stats(const DevBufs &b, uint32_t nscenes, Consts<R> c, in
 cudaError_t launch_slot(const DevBufs &b, uint32_t n, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
-    k_slot<GRID_PER><<<nblk(n, 256 * GRID_PER), 256, 0, st>>>(b.cid_u, n, b.start, b.count, b.tmp);
+    k_slot<SLOT_PER><<<nblk(n, 256 * SLOT_PER), 256, 0, st>>>(b.cid_u, n, b.start, b.count, b.tmp);
     return launch_sort_big(b.start, b.tmp, b.big, st);
 }
 

@@ -77,43 +77,29 @@ __device__ __forceinline__ uint4 make_record(uint2 g, float vx, float vy, float 
 }
 
 // ---- grid: canonical rank + permute, writing the master state and the gather records ----
-// P particles per thread, one from each of the block's P consecutive tiles of 256, so that their
-// dependent loads overlap (as the plain form's k_rank_permute).
-template <int P>
+// (the state loads issued before the rank is counted, as in the plain form's k_rank_permute)
 __global__ void __launch_bounds__(256) k_rank_permute_mixed(
     const uint2 *__restrict__ cid_u, uint32_t n, const uint32_t *__restrict__ start, const uint32_t *__restrict__ tmp,
     const Vec4<float> *__restrict__ pos_u, const Vec4<float> *__restrict__ lo_u, const Vec4<float> *__restrict__ vel_u,
     const SceneDev *__restrict__ scenes, Consts<float> c, MixConsts mc, Vec4<float> *__restrict__ pos_s,
     Vec4<float> *__restrict__ lo_s, Vec4<float> *__restrict__ vel_s, uint2 *__restrict__ gpos)
 {
-    uint32_t idx[P], b[P], e[P];
-    uint2 cd[P];
-#pragma unroll
-    for (int k = 0; k < P; k++) {
-        idx[k] = (blockIdx.x * P + k) * 256u + threadIdx.x;
-        if (idx[k] < n) cd[k] = cid_u[idx[k]];
-    }
-#pragma unroll
-    for (int k = 0; k < P; k++)
-        if (idx[k] < n) {
-            b[k] = start[cd[k].x];
-            e[k] = start[cd[k].x + 1];
-        }
-#pragma unroll
-    for (int k = 0; k < P; k++) {
-        if (idx[k] >= n || !sph_check(b[k] <= e[k] && e[k] <= n, CHK_SORT)) continue;
-        const uint32_t dst = b[k] + rank_in_cell(tmp, b[k], e[k], cd[k].y);
-        if (!sph_check(dst < e[k], CHK_SORT)) continue;
-        const Vec4<float> p = ld4(pos_u + idx[k]), lo = ld4(lo_u + idx[k]), v = ld4(vel_u + idx[k]);
-        st4(pos_s + dst, p);
-        st4(lo_s + dst, lo);
-        st4(vel_s + dst, v);
-        const SceneDev sc = load_scene(scenes, wbits(p.w));
-        const uint32_t qx = axis_code(p.x, lo.x, sc.half[0], c.h, c.inv_h_f, mc.to_units);
-        const uint32_t qy = axis_code(p.y, lo.y, sc.half[1], c.h, c.inv_h_f, mc.to_units);
-        const uint32_t qz = axis_code(p.z, lo.z, sc.half[2], c.h, c.inv_h_f, mc.to_units);
-        gpos[dst] = make_uint2(qx | (qy << 16), qz);
-    }
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint2 cd = cid_u[i];
+    const Vec4<float> p = ld4(pos_u + i), lo = ld4(lo_u + i), v = ld4(vel_u + i);
+    const uint32_t b = start[cd.x], e = start[cd.x + 1];
+    if (!sph_check(b <= e && e <= n, CHK_SORT)) return;
+    const uint32_t dst = b + rank_in_cell(tmp, b, e, cd.y);
+    if (!sph_check(dst < e, CHK_SORT)) return;
+    st4(pos_s + dst, p);
+    st4(lo_s + dst, lo);
+    st4(vel_s + dst, v);
+    const SceneDev sc = load_scene(scenes, wbits(p.w));
+    const uint32_t qx = axis_code(p.x, lo.x, sc.half[0], c.h, c.inv_h_f, mc.to_units);
+    const uint32_t qy = axis_code(p.y, lo.y, sc.half[1], c.h, c.inv_h_f, mc.to_units);
+    const uint32_t qz = axis_code(p.z, lo.z, sc.half[2], c.h, c.inv_h_f, mc.to_units);
+    gpos[dst] = make_uint2(qx | (qy << 16), qz);
 }
 
 // Kahan step with explicitly rounded operations (no reassociation, no fused multiply-add)
@@ -350,11 +336,10 @@ static inline unsigned nblk(uint32_t n, unsigned t) { return (unsigned) ((n + t 
 cudaError_t mixed_permute(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
-    constexpr int P = 4;  // particles per thread
-    k_rank_permute_mixed<P><<<nblk(n, 256 * P), 256, 0, st>>>(b.cid_u, n, b.start, b.tmp, (const Vec4<float> *) b.pos_u,
-                                                              (const Vec4<float> *) b.lo_u, (const Vec4<float> *) b.vel_u,
-                                                              b.scenes, c, mc, (Vec4<float> *) b.pos_s,
-                                                              (Vec4<float> *) b.lo_s, (Vec4<float> *) b.vel_s, b.gpos);
+    k_rank_permute_mixed<<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.start, b.tmp, (const Vec4<float> *) b.pos_u,
+                                                       (const Vec4<float> *) b.lo_u, (const Vec4<float> *) b.vel_u,
+                                                       b.scenes, c, mc, (Vec4<float> *) b.pos_s,
+                                                       (Vec4<float> *) b.lo_s, (Vec4<float> *) b.vel_s, b.gpos);
     return cudaGetLastError();
 }
 
