@@ -40,6 +40,35 @@ __device__ __forceinline__ bool sph_check(bool, unsigned) { return true; }
     cudaError_t name(uint32_t *) { return cudaSuccess; }
 #endif
 
+// ---- chained launches (programmatic dependent launch) between the step's kernels: a kernel
+// launched by launch_chained may be scheduled while its predecessor in the stream is still
+// draining. Such a kernel must call chain_wait() before anything else: it returns once the
+// predecessor has completed and its writes are visible (griddepcontrol.wait), then lets the
+// next chained kernel be scheduled. Since every chained kernel waits first, each completes only
+// after its predecessor, and the stream's order holds transitively. A kernel launched the
+// ordinary way passes through chain_wait() at once.
+__device__ __forceinline__ void chain_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... K, typename... A>
+inline cudaError_t launch_chained(void (*kernel)(K...), unsigned grid, unsigned block, cudaStream_t st, A... args)
+{
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, ((K) args)...);
+}
+
 template <class R>
 struct alignas(4 * sizeof(R)) Vec4 {
     R x, y, z, w;

@@ -126,6 +126,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *__
                                                               uint32_t *__restrict__ bsum, bool vec,
                                                               uint32_t *__restrict__ big)
 {
+    chain_wait();
     if (big && blockIdx.x == 0 && threadIdx.x == 0) big[0] = 0;  // the apply phase lists this step's big cells
     const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
     const uint4 c4 = load_counts4(count, base, ncells, vec);
@@ -148,6 +149,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t *__r
                                                              uint32_t *__restrict__ start, bool vec,
                                                              uint32_t *__restrict__ big)
 {
+    chain_wait();
     const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
     const uint4 c4 = load_counts4(count, base, ncells, vec);
     // this tile's offset: the sum of the earlier tiles' sums (a few thousand words at most)
@@ -198,6 +200,7 @@ __global__ void __launch_bounds__(256) k_slot(const uint2 *__restrict__ cid_u, u
                                               const uint32_t *__restrict__ start, uint32_t *__restrict__ count,
                                               uint32_t *__restrict__ tmp)
 {
+    chain_wait();
     const unsigned lane = threadIdx.x & 31u;
     uint2 cd[P];
 #pragma unroll
@@ -237,6 +240,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_big(const uint32_t *__res
                                                            const uint32_t *__restrict__ big)
 {
     __shared__ uint32_t sk[kBigCellMax];
+    chain_wait();
     const uint32_t nbig = big[0];
     for (uint32_t q = blockIdx.x; q < nbig; q += gridDim.x) {
         const uint32_t cell = big[1 + q];
@@ -274,6 +278,7 @@ __global__ void __launch_bounds__(256) k_rank_permute(const uint2 *__restrict__ 
                                                       const Vec4<R> *__restrict__ vel_u,
                                                       Vec4<R> *__restrict__ pos_s, Vec4<R> *__restrict__ vel_s)
 {
+    chain_wait();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 cd = cid_u[i];
@@ -437,6 +442,7 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
                                                       Vec4<R> *__restrict__ frec)
 {
     using St = Stencil<RAD>;
+    chain_wait();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const Vec4<R> pi = ld4(pos + i);
@@ -563,6 +569,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_forces_mask2(
     uint2 *__restrict__ cid_out, uint32_t *__restrict__ count)
 {
     using St = Stencil<RAD>;
+    chain_wait();
     const uint32_t i = blockIdx.x * BLOCK + threadIdx.x;
     if (i >= n) return;
     const Vec4<R> pi = ld4(pos + i);
@@ -938,22 +945,21 @@ cudaError_t Launch<R>::scan(const DevBufs &b, uint32_t ncells, cudaStream_t st)
     const uint32_t nb = (ncells + SCAN_TILE - 1) / SCAN_TILE;
     // 16-byte accesses only where both arrays allow them (a caller's start array may not)
     const bool vec = ((reinterpret_cast<uintptr_t>(b.count) | reinterpret_cast<uintptr_t>(b.start)) & 15u) == 0;
-    k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, vec, b.big);
-    k_scan_apply<<<nb, SCAN_THREADS, 0, st>>>(b.count, ncells, b.bsum, b.start, vec, b.big);
-    return cudaGetLastError();
+    cudaError_t e = launch_chained(k_scan_reduce, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, vec, b.big);
+    if (e == cudaSuccess)
+        e = launch_chained(k_scan_apply, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, b.start, vec, b.big);
+    return e;
 }
 
 template <class R>
 cudaError_t Launch<R>::permute(const DevBufs &b, uint32_t n, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
-    k_slot<SLOT_PER><<<nblk(n, 256 * SLOT_PER), 256, 0, st>>>(b.cid_u, n, b.start, b.count, b.tmp);
-    cudaError_t e = launch_sort_big(b.start, b.tmp, b.big, st);
+    cudaError_t e = launch_slot(b, n, st);
     if (e != cudaSuccess) return e;
-    k_rank_permute<R><<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.start, b.tmp, (const Vec4<R> *) b.pos_u,
-                                                    (const Vec4<R> *) b.vel_u, (Vec4<R> *) b.pos_s,
-                                                    (Vec4<R> *) b.vel_s);
-    return cudaGetLastError();
+    return launch_chained(k_rank_permute<R>, nblk(n, 256), 256, st, b.cid_u, n, b.start, b.tmp,
+                          (const Vec4<R> *) b.pos_u, (const Vec4<R> *) b.vel_u, (Vec4<R> *) b.pos_s,
+                          (Vec4<R> *) b.vel_s);
 }
 
 template <class R>
@@ -978,13 +984,13 @@ cudaError_t Launch<R>::density(const DevBufs &b, uint32_t n, Consts<R> c, const 
     if (t.forces_mode >= 7) {  // masks and force records
         if (t.cell_mult == 2) {
             if constexpr (sizeof(R) == 4)
-                k_density_mask<R, true, 2><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c, b.masks,
-                                                                         (const Vec4<R> *) b.vel_s, (Vec4<R> *) b.frec);
+                return launch_chained(k_density_mask<R, true, 2>, nblk(n, 256), 256, st, pos, aux, b.start, b.scenes,
+                                      n, c, b.masks, (const Vec4<R> *) b.vel_s, (Vec4<R> *) b.frec);
             else
                 return cudaErrorInvalidValue;  // the FP64 form runs on the reference's grid only
         } else {
-            k_density_mask<R, true><<<nblk(n, 256), 256, 0, st>>>(pos, aux, b.start, b.scenes, n, c, b.masks,
-                                                                  (const Vec4<R> *) b.vel_s, (Vec4<R> *) b.frec);
+            return launch_chained(k_density_mask<R, true, 1>, nblk(n, 256), 256, st, pos, aux, b.start, b.scenes, n,
+                                  c, b.masks, (const Vec4<R> *) b.vel_s, (Vec4<R> *) b.frec);
         }
         return cudaGetLastError();
     }
@@ -1005,11 +1011,12 @@ cudaError_t Launch<R>::density(const DevBufs &b, uint32_t n, Consts<R> c, const 
 
 // the record-reading force kernel of one (register budget, block size, stencil) choice
 template <class R, int MINB, int BLOCK, int RAD>
-static void launch_forces_rec(const DevBufs &b, uint32_t n, Consts<R> c, Vec4<R> *ao, cudaStream_t st)
+static cudaError_t launch_forces_rec(const DevBufs &b, uint32_t n, Consts<R> c, Vec4<R> *ao, cudaStream_t st)
 {
-    k_forces_mask2<R, MINB, true, BLOCK, RAD><<<nblk(n, BLOCK), BLOCK, 0, st>>>(
-        (const Vec4<R> *) b.pos_s, (const Vec4<R> *) b.vel_s, (const Vec4<R> *) b.aux, b.start, b.scenes, b.obstacles,
-        n, c, b.masks, (const Vec4<R> *) b.frec, (Vec4<R> *) b.pos_u, (Vec4<R> *) b.vel_u, ao, b.cid_u, b.count);
+    return launch_chained(k_forces_mask2<R, MINB, true, BLOCK, RAD>, nblk(n, BLOCK), BLOCK, st,
+                          (const Vec4<R> *) b.pos_s, (const Vec4<R> *) b.vel_s, (const Vec4<R> *) b.aux, b.start,
+                          b.scenes, b.obstacles, n, c, b.masks, (const Vec4<R> *) b.frec, (Vec4<R> *) b.pos_u,
+                          (Vec4<R> *) b.vel_u, ao, b.cid_u, b.count);
 }
 
 template <class R>
@@ -1022,14 +1029,13 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
     if (t.cell_mult == 2) {  // cells of h/2: the record variants 7 to 11 (plain FP32 only)
         if constexpr (sizeof(R) == 4) {
             switch (t.forces_mode) {
-            case 7: launch_forces_rec<R, 1, 256, 2>(b, n, c, ao, st); break;
-            case 8: launch_forces_rec<R, 5, 256, 2>(b, n, c, ao, st); break;
-            case 9: launch_forces_rec<R, 6, 256, 2>(b, n, c, ao, st); break;
-            case 10: launch_forces_rec<R, 12, 128, 2>(b, n, c, ao, st); break;
-            case 11: launch_forces_rec<R, 10, 128, 2>(b, n, c, ao, st); break;
+            case 7: return launch_forces_rec<R, 1, 256, 2>(b, n, c, ao, st);
+            case 8: return launch_forces_rec<R, 5, 256, 2>(b, n, c, ao, st);
+            case 9: return launch_forces_rec<R, 6, 256, 2>(b, n, c, ao, st);
+            case 10: return launch_forces_rec<R, 12, 128, 2>(b, n, c, ao, st);
+            case 11: return launch_forces_rec<R, 10, 128, 2>(b, n, c, ao, st);
             default: return cudaErrorInvalidValue;
             }
-            return cudaGetLastError();
         } else {
             return cudaErrorInvalidValue;
         }
@@ -1055,33 +1061,11 @@ cudaError_t Launch<R>::forces(const DevBufs &b, uint32_t n, Consts<R> c, bool re
         k_forces_mask2<R, 0, false><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n,
                                                                   c, b.masks, nullptr, po, vo, ao, b.cid_u, b.count);
         break;
-    case 7:
-        k_forces_mask2<R, 0, true><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
-                                                                 b.masks, (const Vec4<R> *) b.frec, po, vo, ao,
-                                                                 b.cid_u, b.count);
-        break;
-    case 8:
-        k_forces_mask2<R, 5, true><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
-                                                                 b.masks, (const Vec4<R> *) b.frec, po, vo, ao,
-                                                                 b.cid_u, b.count);
-        break;
-    case 9:
-        k_forces_mask2<R, 6, true><<<nblk(n, 256), 256, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
-                                                                 b.masks, (const Vec4<R> *) b.frec, po, vo, ao,
-                                                                 b.cid_u, b.count);
-        break;
-    case 10:
-        k_forces_mask2<R, 12, true, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles,
-                                                                       n, c, b.masks, (const Vec4<R> *) b.frec, po, vo,
-                                                                       ao, b.cid_u, b.count);
-        break;
-    case 11:
-        k_forces_mask2<R, 10, true, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles,
-                                                                       n, c, b.masks, (const Vec4<R> *) b.frec, po, vo,
-                                                                       ao, b.cid_u, b.count);
-        break;
-
-
+    case 7: return launch_forces_rec<R, 0, 256, 1>(b, n, c, ao, st);
+    case 8: return launch_forces_rec<R, 5, 256, 1>(b, n, c, ao, st);
+    case 9: return launch_forces_rec<R, 6, 256, 1>(b, n, c, ao, st);
+    case 10: return launch_forces_rec<R, 12, 128, 1>(b, n, c, ao, st);
+    case 11: return launch_forces_rec<R, 10, 128, 1>(b, n, c, ao, st);
     case 1:
         k_forces_list<R, 32, 128><<<nblk(n, 128), 128, 0, st>>>(pos, vel, aux, b.start, b.scenes, b.obstacles, n, c,
                                                                   po, vo, ao, b.cid_u, b.count);
@@ -1133,8 +1117,9 @@ cudaError_t Launch<R>::stats(const DevBufs &b, uint32_t nscenes, Consts<R> c, in
 cudaError_t launch_slot(const DevBufs &b, uint32_t n, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
-    k_slot<SLOT_PER><<<nblk(n, 256 * SLOT_PER), 256, 0, st>>>(b.cid_u, n, b.start, b.count, b.tmp);
-    return launch_sort_big(b.start, b.tmp, b.big, st);
+    const cudaError_t e =
+        launch_chained(k_slot<SLOT_PER>, nblk(n, 256 * SLOT_PER), 256, st, b.cid_u, n, b.start, b.count, b.tmp);
+    return e == cudaSuccess ? launch_sort_big(b.start, b.tmp, b.big, st) : e;
 }
 
 cudaError_t launch_sort_big(const uint32_t *start, uint32_t *tmp, const uint32_t *big, cudaStream_t st)
@@ -1142,8 +1127,7 @@ cudaError_t launch_sort_big(const uint32_t *start, uint32_t *tmp, const uint32_t
     if (!big) return cudaSuccess;
     // a fixed grid walks the list (its length is known only on the device); with no big cell
     // every block returns at once
-    k_sort_big<<<152, SORT_THREADS, 0, st>>>(start, tmp, big);
-    return cudaGetLastError();
+    return launch_chained(k_sort_big, 152, SORT_THREADS, st, start, tmp, big);
 }
 
 template struct Launch<float>;

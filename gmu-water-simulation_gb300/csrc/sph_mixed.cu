@@ -84,6 +84,7 @@ __global__ void __launch_bounds__(256) k_rank_permute_mixed(
     const SceneDev *__restrict__ scenes, Consts<float> c, MixConsts mc, Vec4<float> *__restrict__ pos_s,
     Vec4<float> *__restrict__ lo_s, Vec4<float> *__restrict__ vel_s, uint2 *__restrict__ gpos)
 {
+    chain_wait();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 cd = cid_u[i];
@@ -121,6 +122,7 @@ __global__ void __launch_bounds__(128) k_density_mixed(const Vec4<float> *__rest
                                                        const Vec4<float> *__restrict__ vel, uint4 *__restrict__ rec)
 {
     using St = Stencil<RAD>;
+    chain_wait();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const Vec4<float> pi = ld4(pos + i);
@@ -207,6 +209,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_forces_mixed(
     Vec4<float> *__restrict__ lo_out, Vec4<float> *__restrict__ vel_out, Vec4<float> *__restrict__ acc_out,
     uint2 *__restrict__ cid_out, uint32_t *__restrict__ count)
 {
+    chain_wait();
     const uint32_t i = blockIdx.x * BLOCK + threadIdx.x;
     if (i >= n) return;
     const Vec4<float> pi = ld4(pos + i);
@@ -336,11 +339,10 @@ static inline unsigned nblk(uint32_t n, unsigned t) { return (unsigned) ((n + t 
 cudaError_t mixed_permute(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
-    k_rank_permute_mixed<<<nblk(n, 256), 256, 0, st>>>(b.cid_u, n, b.start, b.tmp, (const Vec4<float> *) b.pos_u,
-                                                       (const Vec4<float> *) b.lo_u, (const Vec4<float> *) b.vel_u,
-                                                       b.scenes, c, mc, (Vec4<float> *) b.pos_s,
-                                                       (Vec4<float> *) b.lo_s, (Vec4<float> *) b.vel_s, b.gpos);
-    return cudaGetLastError();
+    return launch_chained(k_rank_permute_mixed, nblk(n, 256), 256, st, b.cid_u, n, b.start, b.tmp,
+                          (const Vec4<float> *) b.pos_u, (const Vec4<float> *) b.lo_u, (const Vec4<float> *) b.vel_u,
+                          b.scenes, c, mc, (Vec4<float> *) b.pos_s, (Vec4<float> *) b.lo_s, (Vec4<float> *) b.vel_s,
+                          b.gpos);
 }
 
 cudaError_t mixed_density(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, int cell_mult,
@@ -348,39 +350,34 @@ cudaError_t mixed_density(const DevBufs &b, uint32_t n, Consts<float> c, MixCons
 {
     if (!n) return cudaSuccess;
     // blocks of 128: the SMs finish the dense and sparse regions more evenly than with 256
-    if (cell_mult == 2)
-        k_density_mixed<2><<<nblk(n, 128), 128, 0, st>>>((const Vec4<float> *) b.pos_s, b.gpos, (Vec4<float> *) b.aux,
-                                                         b.start, b.scenes, n, c, mc, b.masks,
-                                                         (const Vec4<float> *) b.vel_s, (uint4 *) b.frec);
-    else
-        k_density_mixed<1><<<nblk(n, 128), 128, 0, st>>>((const Vec4<float> *) b.pos_s, b.gpos, (Vec4<float> *) b.aux,
-                                                         b.start, b.scenes, n, c, mc, b.masks,
-                                                         (const Vec4<float> *) b.vel_s, (uint4 *) b.frec);
-    return cudaGetLastError();
+    return launch_chained(cell_mult == 2 ? k_density_mixed<2> : k_density_mixed<1>, nblk(n, 128), 128, st,
+                          (const Vec4<float> *) b.pos_s, b.gpos, (Vec4<float> *) b.aux, b.start, b.scenes, n, c, mc,
+                          b.masks, (const Vec4<float> *) b.vel_s, (uint4 *) b.frec);
 }
 
 template <int MINB, int BLOCK, int RAD>
-static void launch_forces_mixed(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, bool record_acc,
-                                cudaStream_t st)
+static cudaError_t launch_forces_mixed(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, bool record_acc,
+                                       cudaStream_t st)
 {
-    k_forces_mixed<MINB, BLOCK, RAD><<<nblk(n, BLOCK), BLOCK, 0, st>>>(
-        (const Vec4<float> *) b.pos_s, (const Vec4<float> *) b.lo_s, (const Vec4<float> *) b.vel_s,
-        (const Vec4<float> *) b.aux, b.gpos, (const uint4 *) b.frec, b.start, b.scenes, b.obstacles, n, c, mc, b.masks,
-        (Vec4<float> *) b.pos_u, (Vec4<float> *) b.lo_u, (Vec4<float> *) b.vel_u,
-        record_acc ? (Vec4<float> *) b.acc : nullptr, b.cid_u, b.count);
+    return launch_chained(
+        k_forces_mixed<MINB, BLOCK, RAD>, nblk(n, BLOCK), BLOCK, st, (const Vec4<float> *) b.pos_s,
+        (const Vec4<float> *) b.lo_s, (const Vec4<float> *) b.vel_s, (const Vec4<float> *) b.aux, b.gpos,
+        (const uint4 *) b.frec, b.start, b.scenes, b.obstacles, n, c, mc, b.masks, (Vec4<float> *) b.pos_u,
+        (Vec4<float> *) b.lo_u, (Vec4<float> *) b.vel_u, record_acc ? (Vec4<float> *) b.acc : nullptr, b.cid_u,
+        b.count);
 }
 
 template <int RAD>
-static void mixed_forces_rad(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, bool record_acc,
-                             int variant, cudaStream_t st)
+static cudaError_t mixed_forces_rad(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, bool record_acc,
+                                    int variant, cudaStream_t st)
 {
     // variants: blocks of 128 threads at most 64 (0) or 48 (1) registers, blocks of 256 threads
     // with no cap (2) or at 48 registers (3); every variant computes the same bits
     switch (variant) {
-    case 1: launch_forces_mixed<10, 128, RAD>(b, n, c, mc, record_acc, st); break;
-    case 2: launch_forces_mixed<1, 256, RAD>(b, n, c, mc, record_acc, st); break;
-    case 3: launch_forces_mixed<5, 256, RAD>(b, n, c, mc, record_acc, st); break;
-    default: launch_forces_mixed<8, 128, RAD>(b, n, c, mc, record_acc, st); break;
+    case 1: return launch_forces_mixed<10, 128, RAD>(b, n, c, mc, record_acc, st);
+    case 2: return launch_forces_mixed<1, 256, RAD>(b, n, c, mc, record_acc, st);
+    case 3: return launch_forces_mixed<5, 256, RAD>(b, n, c, mc, record_acc, st);
+    default: return launch_forces_mixed<8, 128, RAD>(b, n, c, mc, record_acc, st);
     }
 }
 
@@ -388,9 +385,8 @@ cudaError_t mixed_forces(const DevBufs &b, uint32_t n, Consts<float> c, MixConst
                          int cell_mult, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
-    if (cell_mult == 2) mixed_forces_rad<2>(b, n, c, mc, record_acc, variant, st);
-    else mixed_forces_rad<1>(b, n, c, mc, record_acc, variant, st);
-    return cudaGetLastError();
+    return cell_mult == 2 ? mixed_forces_rad<2>(b, n, c, mc, record_acc, variant, st)
+                          : mixed_forces_rad<1>(b, n, c, mc, record_acc, variant, st);
 }
 
 cudaError_t mixed_egress(const DevBufs &b, uint32_t n_state, uint32_t n_aux, uint32_t n_acc, int layout_sorted,
