@@ -263,16 +263,19 @@ def timed_run(ctx, torch, ext, flush, warmup, k, run, on_step=None):
     """Steps a context through `warmup` untimed steps and then a `run`-step run of which the k
     steps of timed_steps(k, run) are timed: per timed step, L2 flushed, then the three passes
     between CUDA events on the library's stream. Returns the per-step event times
-    [(grid, density, forces), ...] and the (force variant, cell multiple) of each timed step
-    (read after the step's grid pass: online tuning may change both between steps)."""
+    [(grid, density, forces), ...], the (force variant, cell multiple) of each timed step and
+    the cell multiple of every step, warm-up included (read after the step's grid pass: online
+    tuning may change both between steps)."""
     chosen = []
+    sched = []
 
     def passes(evs=None):
         if evs is not None:
             evs[0].record(ext)
         ctx.pass_grid()
+        sched.append(ctx.cell_multiple())
         if evs is not None:
-            chosen.append((ctx.variant()[1], ctx.cell_multiple()))
+            chosen.append((ctx.variant()[1], sched[-1]))
             evs[1].record(ext)
         ctx.pass_density()
         if evs is not None:
@@ -304,7 +307,7 @@ def timed_run(ctx, torch, ext, flush, warmup, k, run, on_step=None):
     if on_step:
         on_step("stop")
     times = [(e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), e[2].elapsed_time(e[3])) for e in evs]
-    return times, used
+    return times, used, sched
 
 
 def mixed_leg(sphcuda, torch, pos, vel0, steps, warmup, flush, dev, run=RUN_STEPS):
@@ -319,7 +322,7 @@ def mixed_leg(sphcuda, torch, pos, vel0, steps, warmup, flush, dev, run=RUN_STEP
     ctx.autotune(reps=3)
     ctx.set_online_tuning(50)
     ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
-    times, used = timed_run(ctx, torch, ext, flush, warmup, steps, max(steps, run))
+    times, used, _ = timed_run(ctx, torch, ext, flush, warmup, steps, max(steps, run))
     total_ms = sum(sum(t) for t in times)
     check = fp64_error(sphcuda, ctx, sphcuda.SPH_MIXED, N)
     check["cell_multiple_steps"] = {str(m): sum(1 for u in used if u[1] == m) for m in (1, 2)}
@@ -368,7 +371,7 @@ def batch_leg(sphcuda, torch, steps, warmup, flush, dev):
         ctx.autotune(reps=2)
         ctx.set_online_tuning(50)
         ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
-        times, used = timed_run(ctx, torch, ext, flush, warmup, steps, max(steps, BATCH_RUN_STEPS))
+        times, used, _ = timed_run(ctx, torch, ext, flush, warmup, steps, max(steps, BATCH_RUN_STEPS))
         total_ms = sum(sum(t) for t in times)
         res[name] = {"value": N * len(times) / (total_ms / 1000.0), "ms_per_step": total_ms / len(times),
                      "cell_multiple_steps": {str(m): sum(1 for u in used if u[1] == m) for m in (1, 2)},
@@ -730,7 +733,7 @@ def main():
         else:
             t_wall[0] = time.perf_counter() - t_wall[0]
 
-    times, used = timed_run(ctx, torch, ext, flush, args.warmup, args.steps, run, on_step)
+    times, used, sched = timed_run(ctx, torch, ext, flush, args.warmup, args.steps, run, on_step)
     clk = clocks.stop()
     K = len(times)
     grid_ms = [t[0] for t in times]
@@ -780,9 +783,16 @@ def main():
              torch.empty((N, 3), dtype=torch.float32).pin_memory())]
     counts = np.array([N], np.uint32)
 
+    # the resident run's cell multiple of every step (its first, untimed step included), replayed:
+    # the multiple sets the order of each particle's sums, so the same schedule gives the same
+    # bits, while the force variants, re-timed online, do not change them
+    sched = [cell_mult] + sched
+
     def e2e_step(k):
         src, dst = bufs[k % 2], bufs[(k + 1) % 2]
         ctx.upload_raw(src[0].data_ptr(), src[1].data_ptr(), counts)
+        if ctx.cell_multiple() != sched[k]:
+            ctx.set_cell_multiple(sched[k])
         ctx.step(1)
         ctx.download_raw(dst[0].data_ptr(), dst[1].data_ptr())
 
