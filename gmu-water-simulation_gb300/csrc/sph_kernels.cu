@@ -68,12 +68,14 @@ __global__ void __launch_bounds__(256) k_ingest(Vec4<R> *__restrict__ pos_u, Vec
 // Replaces scan_local / increment_local_scans (resources/kernels/sph_grid.cl:71-121, 9-23)
 // and its sums-buffer race. The counts are left as they are: the slot pass takes every slot
 // by decrementing its cell's count, which leaves the counts at zero for the next hash.
-// 1024-cell tiles (256 threads x 4 cells, one 16-byte access per array and thread): enough
-// blocks to fill the GPU on grids of a few hundred thousand cells.
+// A tile is Q groups of 256 x 4 cells: each thread reads one 16-byte group of 4 counts per
+// group (coalesced across the block) and the groups are scanned one after another. Q = 1 (1024
+// cells) gives enough blocks to fill the GPU on grids of a few hundred thousand cells; grids of
+// millions of cells (cells of h/2) take Q = 4, four 16-byte loads in flight per thread.
 constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_PER = 4;
-constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER;
-static_assert(SCAN_TILE == (int) kScanTile, "the scan tile and the block-sum sizing agree");
+constexpr int SCAN_GROUP = SCAN_THREADS * 4;
+constexpr uint32_t kScanLargeGrid = 1u << 21;  // cells from which tiles of 4 groups are used
+static_assert(SCAN_GROUP == (int) kScanTile, "the smallest scan tile and the block-sum sizing agree");
 
 // the 4 counts of a thread, 0 beyond ncells; one 16-byte load when the array is 16-byte
 // aligned (vec, decided on the host from the pointers), else 4 scalar loads
@@ -122,15 +124,20 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &t
     return excl;
 }
 
+template <int Q>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *__restrict__ count, uint32_t ncells,
                                                               uint32_t *__restrict__ bsum, bool vec,
                                                               uint32_t *__restrict__ big)
 {
     chain_wait();
     if (big && blockIdx.x == 0 && threadIdx.x == 0) big[0] = 0;  // the apply phase lists this step's big cells
-    const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
-    const uint4 c4 = load_counts4(count, base, ncells, vec);
-    uint32_t s = c4.x + c4.y + c4.z + c4.w;
+    uint4 c4[Q];
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+        c4[q] = load_counts4(count, (blockIdx.x * Q + q) * SCAN_GROUP + threadIdx.x * 4, ncells, vec);
+    uint32_t s = 0;
+#pragma unroll
+    for (int q = 0; q < Q; q++) s += c4[q].x + c4[q].y + c4[q].z + c4[q].w;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     __shared__ uint32_t w[SCAN_THREADS / 32];
@@ -144,14 +151,17 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *__
     }
 }
 
+template <int Q>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t *__restrict__ count, uint32_t ncells,
                                                              const uint32_t *__restrict__ bsum,
                                                              uint32_t *__restrict__ start, bool vec,
                                                              uint32_t *__restrict__ big)
 {
     chain_wait();
-    const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
-    const uint4 c4 = load_counts4(count, base, ncells, vec);
+    uint4 c4[Q];
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+        c4[q] = load_counts4(count, (blockIdx.x * Q + q) * SCAN_GROUP + threadIdx.x * 4, ncells, vec);
     // this tile's offset: the sum of the earlier tiles' sums (a few thousand words at most)
     __shared__ uint32_t off_w[SCAN_THREADS / 32];
     uint32_t part = 0;
@@ -163,22 +173,28 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t *__r
     uint32_t off = 0;
 #pragma unroll
     for (int w = 0; w < SCAN_THREADS / 32; w++) off += off_w[w];
-    uint32_t total;
-    const uint32_t run = block_exclusive_scan(c4.x + c4.y + c4.z + c4.w, total) + off;
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) start[ncells] = off + total;
-    const uint4 st4v = make_uint4(run, run + c4.x, run + c4.x + c4.y, run + c4.x + c4.y + c4.z);
-    if (big) {  // cells above kBigCell particles get their slot ids sorted before the rank
-        const uint32_t cv[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
-        for (int k = 0; k < 4; k++)
-            if (cv[k] > kBigCell) big[1 + atomicAdd(big, 1u)] = base + (uint32_t) k;
+    for (int q = 0; q < Q; q++) {  // the groups in order, each offset by the ones before it
+        const uint4 c = c4[q];
+        const uint32_t base = (blockIdx.x * Q + q) * SCAN_GROUP + threadIdx.x * 4;
+        uint32_t total;
+        const uint32_t run = block_exclusive_scan(c.x + c.y + c.z + c.w, total) + off;
+        off += total;
+        const uint4 st4v = make_uint4(run, run + c.x, run + c.x + c.y, run + c.x + c.y + c.z);
+        if (big) {  // cells above kBigCell particles get their slot ids sorted before the rank
+            const uint32_t cv[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (cv[k] > kBigCell) big[1 + atomicAdd(big, 1u)] = base + (uint32_t) k;
+        }
+        if (vec && base + 4 <= ncells) {
+            *reinterpret_cast<uint4 *>(start + base) = st4v;
+        } else {
+            const uint32_t sv[4] = {st4v.x, st4v.y, st4v.z, st4v.w};
+            for (uint32_t k = 0; k < 4 && base + k < ncells; k++) start[base + k] = sv[k];
+        }
     }
-    if (vec && base + 4 <= ncells) {
-        *reinterpret_cast<uint4 *>(start + base) = st4v;
-    } else {
-        const uint32_t sv[4] = {st4v.x, st4v.y, st4v.z, st4v.w};
-        for (uint32_t k = 0; k < 4 && base + k < ncells; k++) start[base + k] = sv[k];
-    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) start[ncells] = off;
 }
 
 // ------------------------------------------------------------------------------------
@@ -942,12 +958,19 @@ cudaError_t Launch<R>::ingest(const DevBufs &b, const float *xyz, const float *v
 template <class R>
 cudaError_t Launch<R>::scan(const DevBufs &b, uint32_t ncells, cudaStream_t st)
 {
-    const uint32_t nb = (ncells + SCAN_TILE - 1) / SCAN_TILE;
     // 16-byte accesses only where both arrays allow them (a caller's start array may not)
     const bool vec = ((reinterpret_cast<uintptr_t>(b.count) | reinterpret_cast<uintptr_t>(b.start)) & 15u) == 0;
-    cudaError_t e = launch_chained(k_scan_reduce, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, vec, b.big);
+    if (ncells >= kScanLargeGrid) {
+        const uint32_t nb = (ncells + 4 * SCAN_GROUP - 1) / (4 * SCAN_GROUP);
+        cudaError_t e = launch_chained(k_scan_reduce<4>, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, vec, b.big);
+        if (e == cudaSuccess)
+            e = launch_chained(k_scan_apply<4>, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, b.start, vec, b.big);
+        return e;
+    }
+    const uint32_t nb = (ncells + SCAN_GROUP - 1) / SCAN_GROUP;
+    cudaError_t e = launch_chained(k_scan_reduce<1>, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, vec, b.big);
     if (e == cudaSuccess)
-        e = launch_chained(k_scan_apply, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, b.start, vec, b.big);
+        e = launch_chained(k_scan_apply<1>, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, b.start, vec, b.big);
     return e;
 }
 
