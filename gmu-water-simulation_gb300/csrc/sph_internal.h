@@ -146,8 +146,9 @@ struct Stencil {
 };
 constexpr int kMaskWordsPerParticle = 36;
 
-// Cells per block of the cell-count scan; the block-sum buffer holds one word per tile
-// (plus one) and is sized with this constant wherever it is allocated.
+// Cells of the cell-count scan's smallest tile (one block of 256 threads x 4 cells); larger
+// grids use tiles of several such groups. The block-sum buffer holds one word per tile of this
+// size (plus one), enough for any tile size, and is sized with it wherever it is allocated.
 constexpr uint32_t kScanTile = 1024;
 
 // Cells holding more than kBigCell particles are listed by the scan and their slot ids sorted
