@@ -107,6 +107,33 @@ __device__ __forceinline__ void st4(Vec4<double> *p, Vec4<double> v)
     q[0] = make_double2(v.x, v.y);
     q[1] = make_double2(v.z, v.w);
 }
+// Stores of what the density pass hands to the force pass (the neighbour masks and the force
+// records), marked evict-last in L2 (createpolicy ... L2::evict_last with an L2::cache_hint
+// store): they are read by the very next kernel, while the streams around them are read once.
+__device__ __forceinline__ uint64_t l2_keep_policy()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ void st_keep(uint32_t *a, uint32_t v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(a), "r"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st4_keep(Vec4<float> *p, Vec4<float> v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
+                 "f"(v.w), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ void st4_keep(Vec4<double> *p, Vec4<double> v, uint64_t) { st4(p, v); }
+__device__ __forceinline__ void st_keep(uint4 *p, uint4 v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.v4.b32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z),
+                 "r"(v.w), "l"(pol)
+                 : "memory");
+}
+
 // (q, 1/rho) of a neighbour: the upper half of its aux record
 __device__ __forceinline__ void ld_qinv(const Vec4<float> *p, float &q, float &inv)
 {

@@ -467,6 +467,7 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
     hash_cell<R>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
     const R h2 = c.h2;
     R acc = 0;
+    const uint64_t keep = l2_keep_policy();  // masks and records: read by the force pass next
     const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
     const int xl = cx - RAD > 0 ? cx - RAD : 0, xh = cx + RAD < X ? cx + RAD : X - 1;
 #pragma unroll 1
@@ -493,7 +494,7 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
                     acc = poly6_acc<R>(acc, t);
                 }
                 m >>= 32 - (ce - cb);
-                if (w < St::WORDS) masks[(size_t) (r * St::WORDS + w) * n + i] = m;
+                if (w < St::WORDS) st_keep(masks + (size_t) (r * St::WORDS + w) * n + i, m, keep);
             }
         }
     }
@@ -504,8 +505,8 @@ __global__ void __launch_bounds__(256) k_density_mask(const Vec4<R> *__restrict_
     st4(aux + i, ar);
     if (REC) {  // the force pass's view of this particle as a neighbour, in one 2 x 16-byte record
         const Vec4<R> vi = ld4(vel + i);
-        st4(frec + 2 * (size_t) i, Vec4<R>{pi.x, pi.y, pi.z, q});
-        st4(frec + 2 * (size_t) i + 1, Vec4<R>{vi.x, vi.y, vi.z, inv});
+        st4_keep(frec + 2 * (size_t) i, Vec4<R>{pi.x, pi.y, pi.z, q}, keep);
+        st4_keep(frec + 2 * (size_t) i + 1, Vec4<R>{vi.x, vi.y, vi.z, inv}, keep);
     }
 }
 

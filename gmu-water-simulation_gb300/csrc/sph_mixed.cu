@@ -131,6 +131,7 @@ __global__ void __launch_bounds__(128) k_density_mixed(const Vec4<float> *__rest
     int cx, cy, cz;
     hash_cell<float>(sc, pi.x, pi.y, pi.z, c, cx, cy, cz);
     float sum = 0.0f, comp = 0.0f;
+    const uint64_t keep = l2_keep_policy();  // masks and records: read by the force pass next
     const int X = sc.res[0], Y = sc.res[1], Z = sc.res[2];
     const int xl = cx - RAD > 0 ? cx - RAD : 0, xh = cx + RAD < X ? cx + RAD : X - 1;
 #pragma unroll 1
@@ -159,7 +160,7 @@ __global__ void __launch_bounds__(128) k_density_mixed(const Vec4<float> *__rest
                 }
                 kahan_add(sum, comp, csum);
                 m >>= 32 - (ce - cb);
-                if (w < St::WORDS) masks[(size_t) (r * St::WORDS + w) * n + i] = m;
+                if (w < St::WORDS) st_keep(masks + (size_t) (r * St::WORDS + w) * n + i, m, keep);
             }
         }
     }
@@ -168,7 +169,7 @@ __global__ void __launch_bounds__(128) k_density_mixed(const Vec4<float> *__rest
     const float q = __fdiv_rn(p, __fmul_rn(rho, rho)), inv = __fdiv_rn(1.0f, rho);
     st4(aux + i, Vec4<float>{rho, p, q, inv});
     const Vec4<float> vi = ld4(vel + i);
-    rec[i] = make_record(gi, vi.x, vi.y, vi.z, q, inv);
+    st_keep(rec + i, make_record(gi, vi.x, vi.y, vi.z, q, inv), keep);
 }
 
 // ---- forces: mask-driven, code-unit displacements, one 16-byte record per neighbour ----------
