@@ -134,10 +134,10 @@ MASK_BYTES = 36  # 9 rows x one 32-bit mask word per particle (rest density)
 # force variant 10, keyed by (kernel, cell multiple):
 # profiles/k_forces_mask2_variant10_k_density_mask_step254_dam_break_1m.md (cells of h) and
 # profiles/k_forces_mask2_k_density_mask_half_cells_step254_dam_break_1m.md (cells of h/2)
-TRAFFIC = {("k_forces", 1): 194.83e6, ("k_density", 1): 102.56e6,
-           ("k_forces", 2): 210.24e6, ("k_density", 2): 117.41e6}
-ISSUE = {("k_forces", 1): 388.12e6, ("k_density", 1): 312.25e6,
-         ("k_forces", 2): 300.82e6, ("k_density", 2): 261.00e6}
+TRAFFIC = {("k_forces", 1): 195.87e6, ("k_density", 1): 91.85e6,
+           ("k_forces", 2): 210.64e6, ("k_density", 2): 108.91e6}
+ISSUE = {("k_forces", 1): 395.07e6, ("k_density", 1): 311.76e6,
+         ("k_forces", 2): 300.89e6, ("k_density", 2): 261.09e6}
 TRAFFIC_SOURCE = ("ncu, one launch at step ~254 (the compressed column), force variant 10, on the run's "
                   "main cell multiple: profiles/k_forces_mask2_variant10_k_density_mask_step254_dam_break_1m.md, "
                   "profiles/k_forces_mask2_k_density_mask_half_cells_step254_dam_break_1m.md")
