@@ -130,17 +130,14 @@ MASK_BYTES = 36  # 9 rows x one 32-bit mask word per particle (rest density)
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) and warp instructions
 # (smsp__inst_executed.sum) per launch of the dominant kernels in the compressed column (step ~254
-# of this workload, where most of the run is spent), one ncu capture of each kernel alone with
-# force variant 10, keyed by (kernel, cell multiple):
-# profiles/k_forces_mask2_variant10_k_density_mask_step254_dam_break_1m.md (cells of h) and
-# profiles/k_forces_mask2_k_density_mask_half_cells_step254_dam_break_1m.md (cells of h/2)
+# of this workload, where most of the run is spent): one `ncu --set full` capture of each kernel
+# alone (one launch, cold L2) with force variant 10, keyed by (kernel, cell multiple)
 TRAFFIC = {("k_forces", 1): 195.87e6, ("k_density", 1): 91.85e6,
            ("k_forces", 2): 210.64e6, ("k_density", 2): 108.91e6}
 ISSUE = {("k_forces", 1): 395.07e6, ("k_density", 1): 311.76e6,
          ("k_forces", 2): 300.89e6, ("k_density", 2): 261.09e6}
-TRAFFIC_SOURCE = ("ncu, one launch at step ~254 (the compressed column), force variant 10, on the run's "
-                  "main cell multiple: profiles/k_forces_mask2_variant10_k_density_mask_step254_dam_break_1m.md, "
-                  "profiles/k_forces_mask2_k_density_mask_half_cells_step254_dam_break_1m.md")
+TRAFFIC_SOURCE = ("ncu --set full, one launch of the kernel alone at step ~254 (the compressed column, restarted "
+                  "with --init-state), force variant 10, on the run's main cell multiple, cold L2")
 ISSUE_SOURCE = TRAFFIC_SOURCE
 
 
