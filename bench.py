@@ -56,7 +56,7 @@ DIMS = (100, 100, 100)
 GRAVITY = (0.0, -9.81, 0.0)
 SEED = 1
 H32 = np.float32(0.0457)
-KERNELS_PER_STEP = 7  # scan reduce and apply, slot, crowded-cell sort, rank+permute, density, forces
+KERNELS_PER_STEP = 6  # scan, slot, crowded-cell sort, rank+permute, density, forces
 RUN_STEPS = 500        # the configuration's run
 BATCH_RUN_STEPS = 1000  # the 256-scene batch's run
 SM_COUNT = 152
@@ -111,8 +111,8 @@ def alg_bytes(N, C, rs=4, forces_variant=4):
     r4 = 4 * rs
     rec = 3 * r4 * N if forces_variant >= 7 else 0  # velocity read + 2 x r4 record written
     return {
-        # counts read twice, starts written
-        "scan": 12 * C,
+        # counts read, starts written (the tile offsets come from the per-group counts)
+        "scan": 8 * C,
         # (cell, id) read, id scattered, cell start read, count read-modify-write (back to 0)
         "slot": 12 * N + 12 * C,
         # (cell, id) + the cell's ids read, state read and written in sorted order, starts

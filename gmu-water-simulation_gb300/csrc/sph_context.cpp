@@ -123,9 +123,20 @@ MixConsts make_mix(const sph_params &p)
 }
 size_t r4_bytes(const sph_ctx *c) { return is_f64(c) ? 32 : 16; }
 
-template <class R>
-Consts<R> make_consts(const sph_params &p, int cell_mult = 1)
+// The hash outputs of a grid of ncells cells cleared: the per-cell counts, their per-group sums
+// and the crowded-cell list (the step's own passes leave all three empty between steps).
+int clear_counts(sph_ctx *c, uint64_t ncells)
 {
+    CK(c, cudaMemsetAsync(c->b.count, 0, 4 * ncells, c->stream));
+    CK(c, cudaMemsetAsync(c->b.bsum, 0, 4 * (ncells / kScanTile + 1), c->stream));
+    CK(c, cudaMemsetAsync(c->b.big, 0, 4, c->stream));
+    return SPH_OK;
+}
+
+template <class R>
+Consts<R> make_consts(const sph_ctx *ctx, int cell_mult)
+{
+    const sph_params &p = ctx->prm;
     Consts<R> c{};
     const double h = (double) p.h;
     c.h = (R) p.h;
@@ -149,6 +160,7 @@ Consts<R> make_consts(const sph_params &p, int cell_mult = 1)
     // double divisor by the (power-of-two) multiple, both exactly
     c.inv_cell_f = c.inv_h_f * (float) cell_mult;
     c.cell_d = c.h_d / (double) cell_mult;
+    c.gsum = ctx->b.bsum;
     return c;
 }
 
@@ -310,7 +322,7 @@ int allocate(sph_ctx *c)
             p += kCanaryBytes;
         }
     }
-    CK(c, cudaMemsetAsync(b.count, 0, 4 * C, c->stream));
+    if (int rc = clear_counts(c, C)) return rc;
     CK(c, cudaMemsetAsync(b.aux, 0, r4 * N, c->stream));
     CK(c, cudaMemsetAsync(b.err, 0, 16, c->stream));
     return SPH_OK;
@@ -453,10 +465,10 @@ int run_grid(sph_ctx *c)
 {
     CK(c, Launch<R>::scan(c->b, (uint32_t) c->ctot, c->stream));
     if (is_mixed(c)) {
-        CK(c, launch_slot(c->b, c->n, c->stream));
-        CK(c, mixed_permute(c->b, c->n, make_consts<float>(c->prm, c->tune.cell_mult), make_mix(c->prm), c->stream));
+        CK(c, launch_slot(c->b, c->n, (uint32_t) c->ctot, c->stream));
+        CK(c, mixed_permute(c->b, c->n, make_consts<float>(c, c->tune.cell_mult), make_mix(c->prm), c->stream));
     } else {
-        CK(c, Launch<R>::permute(c->b, c->n, c->stream));
+        CK(c, Launch<R>::permute(c->b, c->n, (uint32_t) c->ctot, c->stream));
     }
     return SPH_OK;
 }
@@ -464,9 +476,9 @@ template <class R>
 int run_density(sph_ctx *c)
 {
     if (is_mixed(c))
-        CK(c, mixed_density(c->b, c->n, make_consts<float>(c->prm, c->tune.cell_mult), make_mix(c->prm),
+        CK(c, mixed_density(c->b, c->n, make_consts<float>(c, c->tune.cell_mult), make_mix(c->prm),
                             c->tune.cell_mult, c->stream));
-    else CK(c, Launch<R>::density(c->b, c->n, make_consts<R>(c->prm, c->tune.cell_mult), c->tune, c->stream));
+    else CK(c, Launch<R>::density(c->b, c->n, make_consts<R>(c, c->tune.cell_mult), c->tune, c->stream));
     return SPH_OK;
 }
 template <class R>
@@ -474,9 +486,9 @@ int run_forces(sph_ctx *c)
 {
     const bool rec = (c->prm.flags & SPH_FLAG_RECORD_ACC) != 0;
     if (is_mixed(c))
-        CK(c, mixed_forces(c->b, c->n, make_consts<float>(c->prm, c->tune.cell_mult), make_mix(c->prm), rec,
+        CK(c, mixed_forces(c->b, c->n, make_consts<float>(c, c->tune.cell_mult), make_mix(c->prm), rec,
                            c->tune.forces_mode, c->tune.cell_mult, c->stream));
-    else CK(c, Launch<R>::forces(c->b, c->n, make_consts<R>(c->prm, c->tune.cell_mult), rec, c->tune, c->stream));
+    else CK(c, Launch<R>::forces(c->b, c->n, make_consts<R>(c, c->tune.cell_mult), rec, c->tune, c->stream));
     return SPH_OK;
 }
 
@@ -722,10 +734,10 @@ int set_cell_mult(sph_ctx *c, int m)
     }
     int rc = upload_scenes(c);  // also sets c->ctot
     if (rc) return rc;
-    CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
+    if (int rc2 = clear_counts(c, c->ctot)) return rc2;
     if (c->state == HASHED && c->n) {
-        if (is_f64(c)) CK(c, Launch<double>::rehash(c->b, c->n, make_consts<double>(c->prm, m), c->stream));
-        else CK(c, Launch<float>::rehash(c->b, c->n, make_consts<float>(c->prm, m), c->stream));
+        if (is_f64(c)) CK(c, Launch<double>::rehash(c->b, c->n, make_consts<double>(c, m), c->stream));
+        else CK(c, Launch<float>::rehash(c->b, c->n, make_consts<float>(c, m), c->stream));
     }
     return SPH_OK;
 }
@@ -738,9 +750,9 @@ int refill_unsorted(sph_ctx *c)
     CK(c, cudaMemcpyAsync(c->b.pos_u, c->b.pos_s, r4 * c->n, cudaMemcpyDeviceToDevice, c->stream));
     CK(c, cudaMemcpyAsync(c->b.vel_u, c->b.vel_s, r4 * c->n, cudaMemcpyDeviceToDevice, c->stream));
     if (is_mixed(c)) CK(c, cudaMemcpyAsync(c->b.lo_u, c->b.lo_s, 16ull * c->n, cudaMemcpyDeviceToDevice, c->stream));
-    CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
-    if (is_f64(c)) CK(c, Launch<double>::rehash(c->b, c->n, make_consts<double>(c->prm, c->tune.cell_mult), c->stream));
-    else CK(c, Launch<float>::rehash(c->b, c->n, make_consts<float>(c->prm, c->tune.cell_mult), c->stream));
+    if (int rc = clear_counts(c, c->ctot)) return rc;
+    if (is_f64(c)) CK(c, Launch<double>::rehash(c->b, c->n, make_consts<double>(c, c->tune.cell_mult), c->stream));
+    else CK(c, Launch<float>::rehash(c->b, c->n, make_consts<float>(c, c->tune.cell_mult), c->stream));
     c->state = HASHED;
     return SPH_OK;
 }
@@ -888,7 +900,7 @@ int sph_upload(sph_ctx *c, const float *xyz, const float *vel, const uint32_t *c
         }
         int rc = upload_scene_off(c);
         if (rc) return rc;
-        CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
+        if (int rc2 = clear_counts(c, c->ctot)) return rc2;
         if (total) {
             if (is_mixed(c)) CK(c, cudaMemsetAsync(c->b.lo_u, 0, 16 * total, c->stream));
             // pinned caller arrays are read by the ingest kernel itself; others go through staging
@@ -902,10 +914,10 @@ int sph_upload(sph_ctx *c, const float *xyz, const float *vel, const uint32_t *c
             }
             if (is_f64(c))
                 CK(c, Launch<double>::ingest(c->b, sx, sv, 0, c->n, -1, 0, (uint32_t) c->sc.size(),
-                                             make_consts<double>(c->prm, c->tune.cell_mult), c->stream));
+                                             make_consts<double>(c, c->tune.cell_mult), c->stream));
             else
                 CK(c, Launch<float>::ingest(c->b, sx, sv, 0, c->n, -1, 0, (uint32_t) c->sc.size(),
-                                            make_consts<float>(c->prm, c->tune.cell_mult), c->stream));
+                                            make_consts<float>(c, c->tune.cell_mult), c->stream));
         }
         c->state = HASHED;
         c->n_sorted = 0;
@@ -939,10 +951,10 @@ int append_ingest(sph_ctx *c, uint32_t scene, uint32_t n, bool has_vel)
     if (is_mixed(c)) CK(c, cudaMemsetAsync((char *) c->b.lo_u + 16ull * c->n, 0, 16ull * n, c->stream));
     if (is_f64(c))
         CK(c, Launch<double>::ingest(c->b, c->b.st_xyz, has_vel ? c->b.st_vel : nullptr, c->n, n, (int32_t) scene,
-                                     h.count, (uint32_t) c->sc.size(), make_consts<double>(c->prm, c->tune.cell_mult), c->stream));
+                                     h.count, (uint32_t) c->sc.size(), make_consts<double>(c, c->tune.cell_mult), c->stream));
     else
         CK(c, Launch<float>::ingest(c->b, c->b.st_xyz, has_vel ? c->b.st_vel : nullptr, c->n, n, (int32_t) scene,
-                                    h.count, (uint32_t) c->sc.size(), make_consts<float>(c->prm, c->tune.cell_mult), c->stream));
+                                    h.count, (uint32_t) c->sc.size(), make_consts<float>(c, c->tune.cell_mult), c->stream));
     h.count += n;
     c->n += n;
     c->appended = true;
@@ -1199,7 +1211,7 @@ int sph_autotune(sph_ctx *c, int32_t reps)
             c->tune.density_p = g.d;
             c->tune.forces_mode = g.f;
             for (int r = 0; r <= reps; r++) {  // the first run is a warm-up
-                CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));  // the force pass adds to the counts
+                if (int rc2 = clear_counts(c, c->ctot)) return rc2;  // the force pass adds to the counts
                 CK(c, cudaEventRecord(c->ev[0], c->stream));
                 c->state = SORTED;
                 rc = pass_density(c);
@@ -1226,7 +1238,7 @@ int sph_autotune(sph_ctx *c, int32_t reps)
     }
     c->tune.density_p = bd;
     c->tune.forces_mode = bf;
-    CK(c, cudaMemsetAsync(c->b.count, 0, 4 * c->ctot, c->stream));
+    if (int rc2 = clear_counts(c, c->ctot)) return rc2;
     c->state = SORTED;
     int rc = pass_density(c);
     if (!rc) rc = pass_forces(c);
@@ -1593,8 +1605,8 @@ int sph_stats(sph_ctx *c, uint32_t scene, double out[8])
         return fail(c, SPH_ERR_STATE, "statistics need a completed step or a density pass");
     CK(c, cudaSetDevice(c->device));
     const int layout_sorted = c->state == DENSE ? 1 : 0;
-    if (is_f64(c)) CK(c, Launch<double>::stats(c->b, (uint32_t) c->sc.size(), make_consts<double>(c->prm, c->tune.cell_mult), layout_sorted, c->stream));
-    else CK(c, Launch<float>::stats(c->b, (uint32_t) c->sc.size(), make_consts<float>(c->prm, c->tune.cell_mult), layout_sorted, c->stream));
+    if (is_f64(c)) CK(c, Launch<double>::stats(c->b, (uint32_t) c->sc.size(), make_consts<double>(c, c->tune.cell_mult), layout_sorted, c->stream));
+    else CK(c, Launch<float>::stats(c->b, (uint32_t) c->sc.size(), make_consts<float>(c, c->tune.cell_mult), layout_sorted, c->stream));
     CK(c, cudaMemcpyAsync(out, c->b.stats + 8 * scene, 64, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     return SPH_OK;

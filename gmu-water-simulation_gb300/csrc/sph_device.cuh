@@ -285,12 +285,17 @@ __device__ __forceinline__ void accel_of(const Vec4<R> &pi, const Vec4<R> &vi, R
 
 }
 
-// count[cell] += 1 with one atomic per cell among the warp's converged lanes (sorted particles
-// of a warp mostly land in the same few cells)
-__device__ __forceinline__ void count_add(uint32_t *__restrict__ count, uint32_t cell)
+// count[cell] += 1 and gsum[cell / kScanTile] += 1 with one atomic per cell and one per group
+// among the warp's converged lanes (sorted particles of a warp mostly land in the same few cells)
+__device__ __forceinline__ void count_add(uint32_t *__restrict__ count, uint32_t *__restrict__ gsum, uint32_t cell)
 {
-    const unsigned peers = __match_any_sync(__activemask(), cell);
-    if ((int) (threadIdx.x & 31u) == __ffs(peers) - 1) atomicAdd(count + cell, (uint32_t) __popc(peers));
+    const unsigned act = __activemask();
+    const int lane = (int) (threadIdx.x & 31u);
+    const unsigned peers = __match_any_sync(act, cell);
+    if (lane == __ffs(peers) - 1) atomicAdd(count + cell, (uint32_t) __popc(peers));
+    const uint32_t g = cell / kScanTile;
+    const unsigned gpeers = __match_any_sync(act, g);
+    if (lane == __ffs(gpeers) - 1) atomicAdd(gsum + g, (uint32_t) __popc(gpeers));
 }
 
 template <class R>
@@ -314,7 +319,7 @@ __device__ __forceinline__ void finish_particle(uint32_t i, const Vec4<R> &pi, c
     if (acc_out) st4(acc_out + i, Vec4<R>{ax, ay, az, (R) 0});
     int qx, qy, qz;
     const uint32_t cell = hash_cell<R>(sc, nx, ny, nz, c, qx, qy, qz);
-    count_add(count, cell);
+    count_add(count, c.gsum, cell);
     cid_out[i] = make_uint2(cell, wbits(vi.w));
 }
 

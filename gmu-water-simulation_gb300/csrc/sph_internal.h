@@ -44,6 +44,9 @@ struct Consts {
     // and the divisor of its exact double formula
     float inv_cell_f;
     double cell_d;
+    // particles per group of kScanTile cells of the step grid: every hash adds to it beside the
+    // cell's count, the scan reads it for its tile offsets, the crowded-cell sort clears it
+    uint32_t *gsum;
 };
 
 // Buffers of one context, in the layout of the precision form.
@@ -56,7 +59,7 @@ struct DevBufs {
     uint32_t *tmp;         // ids scattered into cell slots, for the canonical rank
     uint32_t *count;       // particles per global cell (hash output; the slot pass counts it back to 0)
     uint32_t *start;       // exclusive scan of count, ncells_total + 1 entries
-    uint32_t *bsum;        // scan block sums
+    uint32_t *bsum;        // particles per kScanTile-cell group (Consts::gsum), ncells / kScanTile + 1 words
     uint32_t *big;         // cells above kBigCell particles: count in word 0, then the cells (big_words(n) words)
     SceneDev *scenes;
     ObstacleDev *obstacles;
@@ -169,7 +172,7 @@ struct Launch {
     static cudaError_t ingest(const DevBufs &b, const float *xyz, const float *vel, uint32_t first, uint32_t n,
                               int32_t scene, uint32_t id0, uint32_t nscenes, Consts<R> c, cudaStream_t st);
     static cudaError_t scan(const DevBufs &b, uint32_t ncells, cudaStream_t st);
-    static cudaError_t permute(const DevBufs &b, uint32_t n, cudaStream_t st);
+    static cudaError_t permute(const DevBufs &b, uint32_t n, uint32_t ncells, cudaStream_t st);
     // positions of the first n *_u particles hashed again into the step grid (after the cell
     // multiple changed): counts and the cells of cid_u
     static cudaError_t rehash(const DevBufs &b, uint32_t n, Consts<R> c, cudaStream_t st);
@@ -183,11 +186,14 @@ struct Launch {
     static cudaError_t stats(const DevBufs &b, uint32_t nscenes, Consts<R> c, int layout_sorted, cudaStream_t st);
 };
 
-// slot assignment of the counting sort alone (the mixed form has its own permute)
-cudaError_t launch_slot(const DevBufs &b, uint32_t n, cudaStream_t st);
+// slot assignment of the counting sort alone (the mixed form has its own permute), on a grid
+// of ncells cells
+cudaError_t launch_slot(const DevBufs &b, uint32_t n, uint32_t ncells, cudaStream_t st);
 
-// sorts the slot ids of every cell the scan listed in big (after the slots are taken)
-cudaError_t launch_sort_big(const uint32_t *start, uint32_t *tmp, const uint32_t *big, cudaStream_t st);
+// sorts the slot ids of every cell the scan listed in big (after the slots are taken) and
+// clears the group sums gsum of a grid of ncells cells
+cudaError_t launch_sort_big(const uint32_t *start, uint32_t *tmp, const uint32_t *big, uint32_t *gsum,
+                            uint32_t ncells, cudaStream_t st);
 
 // disc emitter on the device (sph_emit.cu): n particles into the float3 staging arrays
 cudaError_t launch_emit_fountain(uint64_t seed, uint32_t step, uint32_t n, const float center[3], float radius,
@@ -209,7 +215,7 @@ cudaError_t launch_splat(const DevBufs &b, uint32_t n, int layout_sorted, uint32
                          uint32_t *count, float *depth, cudaStream_t st);
 
 // Working memory of a reference-grid build of n particles and C cells: counts (C words), slot
-// ids (n), scan block sums (C / kScanTile + 1), crowded cells (big_words(n)).
+// ids (n), group sums (C / kScanTile + 1), crowded cells (big_words(n)).
 struct GridScratch {
     uint32_t *count, *tmp, *bsum, *big;
 };

@@ -56,6 +56,7 @@ __global__ void __launch_bounds__(256) k_ingest(Vec4<R> *__restrict__ pos_u, Vec
     int cx, cy, cz;
     const uint32_t cell = hash_cell<R>(sc, x, y, z, c, cx, cy, cz);
     atomicAdd(count + cell, 1u);
+    atomicAdd(c.gsum + cell / kScanTile, 1u);
     const uint32_t i = first + k;
     st4(pos_u + i, Vec4<R>{x, y, z, mkw<R>(s)});
     st4(vel_u + i, Vec4<R>{vx, vy, vz, mkw<R>(id)});
@@ -63,11 +64,13 @@ __global__ void __launch_bounds__(256) k_ingest(Vec4<R> *__restrict__ pos_u, Vec
 }
 
 // ------------------------------------------------------------------------------------
-// Exclusive scan of the per-cell counts into cell starts (per-tile sums, then per tile the
-// offset from the earlier sums and the scan of the tile).
+// Exclusive scan of the per-cell counts into cell starts: each tile's offset is the sum of the
+// group sums before it (every hash adds to its cell's group beside the cell, so no pass over
+// the counts precedes this one), then the tile scans itself.
 // Replaces scan_local / increment_local_scans (resources/kernels/sph_grid.cl:71-121, 9-23)
 // and its sums-buffer race. The counts are left as they are: the slot pass takes every slot
-// by decrementing its cell's count, which leaves the counts at zero for the next hash.
+// by decrementing its cell's count, which leaves the counts at zero for the next hash; the
+// crowded-cell sort clears the group sums.
 // A tile is Q groups of 256 x 4 cells: each thread reads one 16-byte group of 4 counts per
 // group (coalesced across the block) and the groups are scanned one after another. Q = 1 (1024
 // cells) gives enough blocks to fill the GPU on grids of a few hundred thousand cells; grids of
@@ -125,35 +128,8 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &t
 }
 
 template <int Q>
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *__restrict__ count, uint32_t ncells,
-                                                              uint32_t *__restrict__ bsum, bool vec,
-                                                              uint32_t *__restrict__ big)
-{
-    chain_wait();
-    if (big && blockIdx.x == 0 && threadIdx.x == 0) big[0] = 0;  // the apply phase lists this step's big cells
-    uint4 c4[Q];
-#pragma unroll
-    for (int q = 0; q < Q; q++)
-        c4[q] = load_counts4(count, (blockIdx.x * Q + q) * SCAN_GROUP + threadIdx.x * 4, ncells, vec);
-    uint32_t s = 0;
-#pragma unroll
-    for (int q = 0; q < Q; q++) s += c4[q].x + c4[q].y + c4[q].z + c4[q].w;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    __shared__ uint32_t w[SCAN_THREADS / 32];
-    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        uint32_t t = threadIdx.x < SCAN_THREADS / 32 ? w[threadIdx.x] : 0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (threadIdx.x == 0) bsum[blockIdx.x] = t;
-    }
-}
-
-template <int Q>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t *__restrict__ count, uint32_t ncells,
-                                                             const uint32_t *__restrict__ bsum,
+                                                             const uint32_t *__restrict__ gsum,
                                                              uint32_t *__restrict__ start, bool vec,
                                                              uint32_t *__restrict__ big)
 {
@@ -162,10 +138,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t *__r
 #pragma unroll
     for (int q = 0; q < Q; q++)
         c4[q] = load_counts4(count, (blockIdx.x * Q + q) * SCAN_GROUP + threadIdx.x * 4, ncells, vec);
-    // this tile's offset: the sum of the earlier tiles' sums (a few thousand words at most)
+    // this tile's offset: the sum of the earlier groups' sums (a few thousand words at most)
     __shared__ uint32_t off_w[SCAN_THREADS / 32];
     uint32_t part = 0;
-    for (uint32_t t = threadIdx.x; t < blockIdx.x; t += SCAN_THREADS) part += __ldg(bsum + t);
+    for (uint32_t t = threadIdx.x; t < blockIdx.x * Q; t += SCAN_THREADS) part += __ldg(gsum + t);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((threadIdx.x & 31) == 0) off_w[threadIdx.x >> 5] = part;
@@ -253,10 +229,13 @@ __global__ void __launch_bounds__(256) k_slot(const uint2 *__restrict__ cid_u, u
 constexpr int SORT_THREADS = 256;
 
 __global__ void __launch_bounds__(SORT_THREADS) k_sort_big(const uint32_t *__restrict__ start, uint32_t *__restrict__ tmp,
-                                                           const uint32_t *__restrict__ big)
+                                                           const uint32_t *__restrict__ big,
+                                                           uint32_t *__restrict__ gsum, uint32_t ngroups)
 {
     __shared__ uint32_t sk[kBigCellMax];
     chain_wait();
+    // the scan has read the group sums: zero for the next hash
+    for (uint32_t t = blockIdx.x * SORT_THREADS + threadIdx.x; t < ngroups; t += gridDim.x * SORT_THREADS) gsum[t] = 0;
     const uint32_t nbig = big[0];
     for (uint32_t q = blockIdx.x; q < nbig; q += gridDim.x) {
         const uint32_t cell = big[1 + q];
@@ -292,9 +271,11 @@ __global__ void __launch_bounds__(256) k_rank_permute(const uint2 *__restrict__ 
                                                       const uint32_t *__restrict__ tmp,
                                                       const Vec4<R> *__restrict__ pos_u,
                                                       const Vec4<R> *__restrict__ vel_u,
-                                                      Vec4<R> *__restrict__ pos_s, Vec4<R> *__restrict__ vel_s)
+                                                      Vec4<R> *__restrict__ pos_s, Vec4<R> *__restrict__ vel_s,
+                                                      uint32_t *__restrict__ big)
 {
     chain_wait();
+    if (blockIdx.x == 0 && threadIdx.x == 0) big[0] = 0;  // the crowded-cell list is used: empty for the next scan
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 cd = cid_u[i];
@@ -841,6 +822,7 @@ __global__ void __launch_bounds__(256) k_rehash(const Vec4<R> *__restrict__ pos_
     int cx, cy, cz;
     const uint32_t cell = hash_cell<R>(sc, p.x, p.y, p.z, c, cx, cy, cz);
     atomicAdd(count + cell, 1u);
+    atomicAdd(c.gsum + cell / kScanTile, 1u);
     cid_u[i] = make_uint2(cell, wbits(ldc4(vel_u + i).w));
 }
 
@@ -963,27 +945,21 @@ cudaError_t Launch<R>::scan(const DevBufs &b, uint32_t ncells, cudaStream_t st)
     const bool vec = ((reinterpret_cast<uintptr_t>(b.count) | reinterpret_cast<uintptr_t>(b.start)) & 15u) == 0;
     if (ncells >= kScanLargeGrid) {
         const uint32_t nb = (ncells + 4 * SCAN_GROUP - 1) / (4 * SCAN_GROUP);
-        cudaError_t e = launch_chained(k_scan_reduce<4>, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, vec, b.big);
-        if (e == cudaSuccess)
-            e = launch_chained(k_scan_apply<4>, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, b.start, vec, b.big);
-        return e;
+        return launch_chained(k_scan_apply<4>, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, b.start, vec, b.big);
     }
     const uint32_t nb = (ncells + SCAN_GROUP - 1) / SCAN_GROUP;
-    cudaError_t e = launch_chained(k_scan_reduce<1>, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, vec, b.big);
-    if (e == cudaSuccess)
-        e = launch_chained(k_scan_apply<1>, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, b.start, vec, b.big);
-    return e;
+    return launch_chained(k_scan_apply<1>, nb, SCAN_THREADS, st, b.count, ncells, b.bsum, b.start, vec, b.big);
 }
 
 template <class R>
-cudaError_t Launch<R>::permute(const DevBufs &b, uint32_t n, cudaStream_t st)
+cudaError_t Launch<R>::permute(const DevBufs &b, uint32_t n, uint32_t ncells, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
-    cudaError_t e = launch_slot(b, n, st);
+    cudaError_t e = launch_slot(b, n, ncells, st);
     if (e != cudaSuccess) return e;
     return launch_chained(k_rank_permute<R>, nblk(n, 256), 256, st, b.cid_u, n, b.start, b.tmp,
                           (const Vec4<R> *) b.pos_u, (const Vec4<R> *) b.vel_u, (Vec4<R> *) b.pos_s,
-                          (Vec4<R> *) b.vel_s);
+                          (Vec4<R> *) b.vel_s, b.big);
 }
 
 template <class R>
@@ -1138,20 +1114,20 @@ cudaError_t Launch<R>::stats(const DevBufs &b, uint32_t nscenes, Consts<R> c, in
     return cudaGetLastError();
 }
 
-cudaError_t launch_slot(const DevBufs &b, uint32_t n, cudaStream_t st)
+cudaError_t launch_slot(const DevBufs &b, uint32_t n, uint32_t ncells, cudaStream_t st)
 {
     if (!n) return cudaSuccess;
     const cudaError_t e =
         launch_chained(k_slot<SLOT_PER>, nblk(n, 256 * SLOT_PER), 256, st, b.cid_u, n, b.start, b.count, b.tmp);
-    return e == cudaSuccess ? launch_sort_big(b.start, b.tmp, b.big, st) : e;
+    return e == cudaSuccess ? launch_sort_big(b.start, b.tmp, b.big, b.bsum, ncells, st) : e;
 }
 
-cudaError_t launch_sort_big(const uint32_t *start, uint32_t *tmp, const uint32_t *big, cudaStream_t st)
+cudaError_t launch_sort_big(const uint32_t *start, uint32_t *tmp, const uint32_t *big, uint32_t *gsum,
+                            uint32_t ncells, cudaStream_t st)
 {
-    if (!big) return cudaSuccess;
     // a fixed grid walks the list (its length is known only on the device); with no big cell
-    // every block returns at once
-    return launch_chained(k_sort_big, 152, SORT_THREADS, st, start, tmp, big);
+    // every block only clears its share of the group sums
+    return launch_chained(k_sort_big, 152, SORT_THREADS, st, start, tmp, big, gsum, ncells / kScanTile + 1);
 }
 
 template struct Launch<float>;

@@ -82,9 +82,11 @@ __global__ void __launch_bounds__(256) k_rank_permute_mixed(
     const uint2 *__restrict__ cid_u, uint32_t n, const uint32_t *__restrict__ start, const uint32_t *__restrict__ tmp,
     const Vec4<float> *__restrict__ pos_u, const Vec4<float> *__restrict__ lo_u, const Vec4<float> *__restrict__ vel_u,
     const SceneDev *__restrict__ scenes, Consts<float> c, MixConsts mc, Vec4<float> *__restrict__ pos_s,
-    Vec4<float> *__restrict__ lo_s, Vec4<float> *__restrict__ vel_s, uint2 *__restrict__ gpos)
+    Vec4<float> *__restrict__ lo_s, Vec4<float> *__restrict__ vel_s, uint2 *__restrict__ gpos,
+    uint32_t *__restrict__ big)
 {
     chain_wait();
+    if (blockIdx.x == 0 && threadIdx.x == 0) big[0] = 0;  // the crowded-cell list is used: empty for the next scan
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 cd = cid_u[i];
@@ -291,7 +293,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_forces_mixed(
     if (acc_out) st4(acc_out + i, Vec4<float>{ax, ay, az, 0.0f});
     int qx, qy, qz;
     const uint32_t cell = hash_cell<float>(sc2, hx, hy, hz, c, qx, qy, qz);
-    count_add(count, cell);
+    count_add(count, c.gsum, cell);
     cid_out[i] = make_uint2(cell, wbits(vi.w));
 }
 
@@ -343,7 +345,7 @@ cudaError_t mixed_permute(const DevBufs &b, uint32_t n, Consts<float> c, MixCons
     return launch_chained(k_rank_permute_mixed, nblk(n, 256), 256, st, b.cid_u, n, b.start, b.tmp,
                           (const Vec4<float> *) b.pos_u, (const Vec4<float> *) b.lo_u, (const Vec4<float> *) b.vel_u,
                           b.scenes, c, mc, (Vec4<float> *) b.pos_s, (Vec4<float> *) b.lo_s, (Vec4<float> *) b.vel_s,
-                          b.gpos);
+                          b.gpos, b.big);
 }
 
 cudaError_t mixed_density(const DevBufs &b, uint32_t n, Consts<float> c, MixConsts mc, int cell_mult,

@@ -4,7 +4,7 @@
 // already handed its GPU memory to its own pool allocator, or a per-frame callback in a
 // real-time loop, where cudaMalloc/cudaFree would synchronise the device and stall the frame.
 // The caller passes device arrays for the positions and for every output; the kernels'
-// working memory (per-cell counts, per-particle slot ids, scan block sums, the list
+// working memory (per-cell counts, per-particle slot ids, per-group counts, the list
 // of crowded cells) lives in one file-scope device array of fixed size. The array belongs to
 // the library's device code: CUDA creates it on a device when that code is loaded there, which
 // under lazy module loading (the default) is the first call on that device. That first call
@@ -31,9 +31,9 @@ namespace {
 
 constexpr uint32_t kMaxParticles = 1u << 20;
 constexpr uint32_t kMaxCells = 1u << 20;
-constexpr uint32_t kMaxBlocks = kMaxCells / kScanTile + 1;  // scan block sums
+constexpr uint32_t kMaxBlocks = kMaxCells / kScanTile + 1;  // group sums of the scan
 constexpr size_t kBigWords = big_words(kMaxParticles);       // crowded-cell list
-// counts | slot ids | scan block sums | crowded cells, as 32-bit words
+// counts | slot ids | group sums | crowded cells, as 32-bit words
 constexpr size_t kScratchWords = (size_t) kMaxCells + kMaxParticles + kMaxBlocks + kBigWords;
 
 __device__ __align__(256) uint32_t g_grid_scratch[kScratchWords];
@@ -46,7 +46,8 @@ std::mutex g_scratch_mu;
 
 __global__ void __launch_bounds__(256) k_hash_plain_xyz(const float *__restrict__ xyz, uint32_t n, float3 half,
                                                         int3 res, float inv_h, double h_d,
-                                                        uint32_t *__restrict__ out_cell, uint32_t *__restrict__ count)
+                                                        uint32_t *__restrict__ out_cell, uint32_t *__restrict__ count,
+                                                        uint32_t *__restrict__ gsum)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -56,6 +57,7 @@ __global__ void __launch_bounds__(256) k_hash_plain_xyz(const float *__restrict_
     const uint32_t cell = (uint32_t) cx + (uint32_t) cy * (uint32_t) res.x + (uint32_t) cz * (uint32_t) res.x * (uint32_t) res.y;
     out_cell[i] = cell;
     atomicAdd(count + cell, 1u);
+    atomicAdd(gsum + cell / kScanTile, 1u);
 }
 
 // every id takes a slot of its cell, from the top down (the counts end at zero)
@@ -85,8 +87,8 @@ __global__ void __launch_bounds__(256) k_rank_ids(const uint32_t *__restrict__ c
 
 // The reference's grid of n particles (float xyz, id order) in a box of res cells per axis (cells
 // of size h, linear index x + y*X + z*X*Y): the cell of every particle, the cell starts and the
-// ids in ascending (cell, id) order, with the working memory g (counts, slot ids, scan
-// block sums, crowded-cell list) supplied by the caller.
+// ids in ascending (cell, id) order, with the working memory g (counts, slot ids, group sums,
+// crowded-cell list) supplied by the caller.
 cudaError_t ref_grid_build(const float *xyz, uint32_t n, int3 res, float3 half, float h, uint32_t *out_cell,
                            uint32_t *out_start, uint32_t *out_order, const GridScratch &g, cudaStream_t st)
 {
@@ -97,15 +99,19 @@ cudaError_t ref_grid_build(const float *xyz, uint32_t n, int3 res, float3 half, 
     b.bsum = g.bsum;
     b.big = g.big;
     b.start = out_start;
-    // counts must start at zero: the previous call's values remain in the array
+    // counts, group sums and the crowded-cell list start empty (a previous call, or one that
+    // failed, may have left values)
     cudaError_t e = cudaMemsetAsync(b.count, 0, 4 * ncells, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.bsum, 0, 4 * (ncells / kScanTile + 1), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.big, 0, 4, st);
     if (e != cudaSuccess) return e;
     const unsigned blocks = (unsigned) ((n + 255) / 256);
-    if (n) k_hash_plain_xyz<<<blocks, 256, 0, st>>>(xyz, n, half, res, 1.0f / h, (double) h, out_cell, b.count);
+    if (n)
+        k_hash_plain_xyz<<<blocks, 256, 0, st>>>(xyz, n, half, res, 1.0f / h, (double) h, out_cell, b.count, b.bsum);
     e = Launch<float>::scan(b, (uint32_t) ncells, st);  // starts
     if (e == cudaSuccess && n) {
         k_slot_ids<<<blocks, 256, 0, st>>>(out_cell, n, b.start, b.count, b.tmp);
-        e = launch_sort_big(b.start, b.tmp, b.big, st);
+        e = launch_sort_big(b.start, b.tmp, b.big, b.bsum, (uint32_t) ncells, st);
         if (e == cudaSuccess) {
             k_rank_ids<<<blocks, 256, 0, st>>>(out_cell, n, b.start, b.tmp, out_order);
             e = cudaGetLastError();

@@ -25,7 +25,7 @@ def test_reference_arm_line():
 
 
 def test_byte_model_matches_the_documented_totals():
-    """bench.py's algorithmic bytes per step: 360 N + 44 C with the force records (variants 7 and
+    """bench.py's algorithmic bytes per step: 360 N + 40 C with the force records (variants 7 and
     up), the density pass 116 N + 4 C and the force pass 156 N + 12 C; the 1M dam break's cell
     count is 110 x 110 x 55."""
     sys.path.insert(0, ROOT)
@@ -36,7 +36,7 @@ def test_byte_model_matches_the_documented_totals():
     for v in (7, 9, 10, 11):
         ab = bench.alg_bytes(N, C, 4, v)
         assert ab["density"] == 116 * N + 4 * C and ab["forces"] == 156 * N + 12 * C
-        assert sum(ab.values()) == 360 * N + 44 * C
+        assert sum(ab.values()) == 360 * N + 40 * C
     keys = {(k, m) for k in ("k_forces", "k_density") for m in (1, 2)}
     assert set(bench.TRAFFIC) == keys and set(bench.ISSUE) == keys
 
