@@ -55,8 +55,7 @@ __global__ void __launch_bounds__(256) k_ingest(Vec4<R> *__restrict__ pos_u, Vec
     }
     int cx, cy, cz;
     const uint32_t cell = hash_cell<R>(sc, x, y, z, c, cx, cy, cz);
-    atomicAdd(count + cell, 1u);
-    atomicAdd(c.gsum + cell / kScanTile, 1u);
+    count_add(count, c.gsum, cell);
     const uint32_t i = first + k;
     st4(pos_u + i, Vec4<R>{x, y, z, mkw<R>(s)});
     st4(vel_u + i, Vec4<R>{vx, vy, vz, mkw<R>(id)});
@@ -821,8 +820,7 @@ __global__ void __launch_bounds__(256) k_rehash(const Vec4<R> *__restrict__ pos_
     const SceneDev sc = load_scene(scenes, wbits(p.w));
     int cx, cy, cz;
     const uint32_t cell = hash_cell<R>(sc, p.x, p.y, p.z, c, cx, cy, cz);
-    atomicAdd(count + cell, 1u);
-    atomicAdd(c.gsum + cell / kScanTile, 1u);
+    count_add(count, c.gsum, cell);
     cid_u[i] = make_uint2(cell, wbits(ldc4(vel_u + i).w));
 }
 

@@ -56,8 +56,7 @@ __global__ void __launch_bounds__(256) k_hash_plain_xyz(const float *__restrict_
     const int cz = cell_axis(xyz[3 * i + 2], half.z, inv_h, h_d, res.z);
     const uint32_t cell = (uint32_t) cx + (uint32_t) cy * (uint32_t) res.x + (uint32_t) cz * (uint32_t) res.x * (uint32_t) res.y;
     out_cell[i] = cell;
-    atomicAdd(count + cell, 1u);
-    atomicAdd(gsum + cell / kScanTile, 1u);
+    count_add(count, gsum, cell);
 }
 
 // every id takes a slot of its cell, from the top down (the counts end at zero)
