@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(256) k_ingest(Vec4<R> *__restrict__ pos_u, Vec
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_GROUP = SCAN_THREADS * 4;
 constexpr uint32_t kScanLargeGrid = 1u << 21;  // cells from which tiles of 4 groups are used
-static_assert(SCAN_GROUP == (int) kScanTile, "the smallest scan tile and the block-sum sizing agree");
+static_assert(SCAN_GROUP == (int) kScanTile, "the scan group and the group-count sizing agree");
 
 // the 4 counts of a thread, 0 beyond ncells; one 16-byte load when the array is 16-byte
 // aligned (vec, decided on the host from the pointers), else 4 scalar loads
@@ -137,7 +137,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t *__r
 #pragma unroll
     for (int q = 0; q < Q; q++)
         c4[q] = load_counts4(count, (blockIdx.x * Q + q) * SCAN_GROUP + threadIdx.x * 4, ncells, vec);
-    // this tile's offset: the sum of the earlier groups' sums (a few thousand words at most)
+    // this tile's offset: the sum of the earlier groups' counts (ncells / 1024 words at most,
+    // read by every block, so held in L1 and L2)
     __shared__ uint32_t off_w[SCAN_THREADS / 32];
     uint32_t part = 0;
     for (uint32_t t = threadIdx.x; t < blockIdx.x * Q; t += SCAN_THREADS) part += __ldg(gsum + t);
