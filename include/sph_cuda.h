@@ -131,7 +131,9 @@ const char *sph_device_name(const sph_ctx *ctx);
 
 /* The CUDA stream (a cudaStream_t) every call of ctx launches on, for callers that order
  * their own work or record their own events against the step (no reference counterpart:
- * CLWrapper keeps its command queue private, src/CLWrapper.cpp:3-13). */
+ * CLWrapper keeps its command queue private, src/CLWrapper.cpp:3-13). The step's kernels are
+ * chained launches (programmatic dependent launch): each waits for the complete work before
+ * it in the stream, so work a caller enqueues between two calls is ordered as usual. */
 void *sph_stream(const sph_ctx *ctx);
 
 /* Replaces every scene's particles: counts[s] particles for scene s, concatenated
