@@ -84,6 +84,17 @@ def timed_steps(k, run):
     return sorted({(i * run) // k for i in range(k)})
 
 
+def rehash_steps(sched):
+    """Rehash launches inside each step, from the cell multiple of every step: online tuning
+    switches into the other multiple at the start of its trial step and back, if the trial lost,
+    at the end of that same step; other switches happen at the start of the step that follows."""
+    inside = [0] * len(sched)
+    for j in range(len(sched) - 1):
+        if sched[j + 1] != sched[j]:
+            inside[j if j > 0 and sched[j] != sched[j - 1] else j + 1] += 1
+    return inside
+
+
 def grid_cells(box):
     return int(np.prod([int(np.ceil(np.float32(b) / H32)) for b in box]))
 
@@ -731,6 +742,10 @@ def main():
             t_wall[0] = time.perf_counter() - t_wall[0]
 
     times, used, sched = timed_run(ctx, torch, ext, flush, args.warmup, args.steps, run, on_step)
+    # kernels launched in the timed steps: the step's own, plus a rehash for each switch of the
+    # cell multiple that online tuning makes inside a timed step
+    rehashes = rehash_steps(sched)
+    timed_rehash = sum(rehashes[args.warmup + q] for q in timed_steps(args.steps, run))
     clk = clocks.stop()
     K = len(times)
     grid_ms = [t[0] for t in times]
@@ -860,7 +875,7 @@ def main():
         "mixed": mixed,
         "batch": batch,
         "cpu_baseline": cpu,
-        "gpu_launches": KERNELS_PER_STEP * K,
+        "gpu_launches": KERNELS_PER_STEP * K + timed_rehash,
         "launch_variant": {"density": variant[0], "forces": main_v, "cell_multiple_at_start": cell_mult,
                            "forces_steps": {str(v): vs.count(v) for v in sorted(set(vs))},
                            "cell_multiple_steps": {str(m): sum(1 for u in used if u[1] == m) for m in (1, 2)},

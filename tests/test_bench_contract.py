@@ -68,3 +68,15 @@ def test_compulsory_bytes():
     assert cb == {"density": 24 * N, "forces": 72 * N, "step": 196 * N + 12 * C}
     assert bench.timed_steps(20, 500) == list(range(0, 500, 25))
     assert bench.timed_steps(500, 500) == list(range(500))
+
+
+def test_rehash_launch_count():
+    """bench.py's count of rehash launches per step from the cell multiple of every step: a
+    trial on the other multiple switches in at its start and back at its end (two launches in
+    that step); a switch that stays is the next step's one launch."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.rehash_steps([1, 1, 1, 2, 1, 1, 2, 2, 2, 1]) == [0, 0, 0, 2, 0, 0, 1, 0, 0, 1]
+    assert bench.rehash_steps([2, 2, 2]) == [0, 0, 0]
+    assert bench.rehash_steps([]) == []
