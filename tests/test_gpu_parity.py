@@ -441,6 +441,33 @@ def test_graph_replay_matches_passes(sphlib):
         assert np.array_equal(a[k], b[k]), k
 
 
+def test_caller_work_between_chained_passes(sphlib):
+    """The step's kernels are chained launches (each may be scheduled while its predecessor
+    drains, and waits for it before any other instruction). Work a caller enqueues on the
+    context's stream between the passes (a kernel writing 256 MB, an event, a host wait) runs in
+    stream order among them: the results equal those of the passes alone, bit for bit."""
+    import torch
+
+    pos = c0_scene(sphlib, dims=(20, 20, 20))
+    a = gpu_run(sphlib, C0_BOX, pos, steps=12, gravity=G981)
+    ctx = sphlib.SphContext(C0_BOX, pos.shape[0], gravity=G981, flags=2)
+    ctx.upload(pos)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda:0"))
+    filler = torch.empty(64 * 2**20, dtype=torch.float32, device="cuda:0")
+    for k in range(12):
+        for q, p in enumerate((ctx.pass_grid, ctx.pass_density, ctx.pass_forces)):
+            with torch.cuda.stream(ext):
+                filler.fill_(float(k + q))
+                ev = torch.cuda.Event()
+                ev.record(ext)
+            if (k + q) % 5 == 0:
+                ev.synchronize()
+            p()
+    b = ctx.download(acc=True)
+    for key in a:
+        assert np.array_equal(a[key], b[key]), key
+
+
 # ------------------------------------------------------------------------- emitters, interface
 def test_append_between_steps(sphlib, oracle_mod):
     box = (0.6, 0.6, 0.6)
