@@ -134,6 +134,13 @@ __device__ __forceinline__ void st_keep(uint4 *p, uint4 v, uint64_t pol)
                  : "memory");
 }
 
+// The force passes start every row by loading the row's mask word, the head of that row's
+// chain of dependent loads: the next row's word is fetched into L1 while a row is walked.
+__device__ __forceinline__ void prefetch_l1(const void *p)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 // (q, 1/rho) of a neighbour: the upper half of its aux record
 __device__ __forceinline__ void ld_qinv(const Vec4<float> *p, float &q, float &inv)
 {

@@ -232,6 +232,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_forces_mixed(
 #pragma unroll 1
         for (int dy = -RAD; dy <= RAD; dy++) {
             const int r = (dz + RAD) * (2 * RAD + 1) + (dy + RAD);
+            if (r + 1 < St::ROWS) prefetch_l1(masks + (size_t) ((r + 1) * St::WORDS) * n + i);
             const int z = cz + dz, y = cy + dy;
             if (z < 0 || z >= Z || y < 0 || y >= Y) continue;
             const uint32_t row = sc.cell_base + (uint32_t) y * (uint32_t) X + (uint32_t) z * (uint32_t) X * (uint32_t) Y;
